@@ -1,0 +1,170 @@
+/*
+ * tomography_gb300 -- C ABI of the GB300-native forward FDTD fitness path.
+ *
+ * The reference exposes its hot path as two C++ functions with the signature
+ *     double FDTD_GPU(const std::vector<double>& arguments);   FDTD_GPU.cuh:8
+ *     double FDTD_CPU(const std::vector<double>& arguments);   FDTD_CPU.h:8
+ * which tao's particle-swarm / differential-evolution drivers call once per
+ * candidate (test.cxx:94-121).  This header is the C boundary that replaces
+ * them: plain pointers and sizes, integer status codes, no C++ or CUDA types.
+ * The C++ drop-in with the reference's exact signature is declared in
+ * include/tomography_fdtd.hpp and is a thin wrapper over tomo_fitness().
+ *
+ * All entry points return TOMO_OK (0) or a negative tomo_status; the message
+ * of the last failure on the calling thread is returned by tomo_last_error().
+ * A handle may be used from one thread at a time.
+ */
+#ifndef TOMOGRAPHY_GB300_H
+#define TOMOGRAPHY_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum tomo_status {
+    TOMO_OK = 0,
+    TOMO_EINVAL = -1,          /* bad argument (the reference throws std::out_of_range) */
+    TOMO_ENOMEM_BUDGET = -2,   /* request does not fit the device-memory budget          */
+    TOMO_ETIMEOUT = -3,        /* a bounded wait ran out                                 */
+    TOMO_ENUMERIC = -4,        /* non-finite field / fitness detected                    */
+    TOMO_ECUDA = -5,           /* CUDA runtime error (the reference calls exit(-1))      */
+    TOMO_ENOTREADY = -6,       /* serving ticket not finished yet                        */
+    TOMO_ECANCELLED = -7,      /* serving ticket was cancelled                           */
+    TOMO_ENOTARGET = -8        /* fitness requested before a target was set              */
+} tomo_status;
+
+typedef enum tomo_mode {
+    TOMO_MODE_REFERENCE_GPU = 0, /* FDTD_GPU.cu: 3x3 Debye patches, 27 args, 4 plane waves, |D| misfit   */
+    TOMO_MODE_REFERENCE_CPU = 1, /* FDTD_CPU.cxx: 9x9 (eps_r, sigma) patches, 162 args, relative misfit  */
+    TOMO_MODE_BREAST = 2         /* ellipse phantom, point transmitters, receiver traces, trace misfit    */
+} tomo_mode;
+
+typedef enum tomo_precision { TOMO_FP32 = 0, TOMO_FP64 = 1 } tomo_precision;
+
+#define TOMO_MAX_FREQS 32
+
+/* Runtime problem description; the reference fixes all of this at compile
+ * time in FDTD_common.hxx:1-76.  tomo_spec_reference() fills the exact
+ * reference values. */
+typedef struct tomo_spec {
+    int32_t mode;              /* tomo_mode                                          */
+    int32_t precision;         /* tomo_precision of the field updates                */
+    int32_t nx, ny;            /* H grid nx*ny; Ez grid (nx+1)*(ny+1)                */
+    double dx;                 /* cell size [m] (dx = dy)                            */
+    double dt;                 /* time step [s]                                      */
+    int32_t steps;             /* time steps per solve                               */
+    /* CPML (FDTD_GPU.cu:748-806) */
+    int32_t ncpml;
+    double cpml_grading, cpml_sigma_max, cpml_kappa_max, cpml_alpha_max, cpml_alpha_min;
+    double tau;                /* Debye relaxation time [s]                          */
+    /* reference plane-wave modes */
+    double breast_radius;      /* [m]                                                */
+    int32_t npatch;            /* patches per side (3 GPU path, 9 CPU path)          */
+    int32_t n_excitations;     /* plane-wave angles 2*pi*k/n                         */
+    double pw_tau, pw_t0, pw_l;/* fwf(): Gaussian width, delay, offset               */
+    int32_t pw_centred;        /* 1: x - nx/2 (GPU path), 0: raw x (CPU path)        */
+    int32_t nan_clamp;         /* 1: NaN -> 0 as FDTD_GPU.cu:335-350                 */
+    /* breast-imaging phantom */
+    double bg_eps_inf, bg_del_eps, bg_sigma;
+    double disc_radius, disc_eps_inf, disc_del_eps, disc_sigma;
+    int32_t n_ellipses;        /* 8 parameters each: cx, cy, a, b, angle, eps_inf, del_eps, sigma */
+    int32_t n_antennas;        /* ring of point transmitters / receivers             */
+    int32_t n_tx;              /* transmitters fired per candidate (<= n_antennas)   */
+    double antenna_radius;     /* [m]                                                */
+    double src_f0, src_tau, src_t0, src_amp;  /* modulated Gaussian current source; amp 0 = auto */
+    /* near-to-far-field transform */
+    int32_t nf2ff_d;           /* contour distance from the grid edge [cells]        */
+    int32_t nfreq;
+    double freqs[TOMO_MAX_FREQS];
+    int32_t n_angles;
+    int32_t ff_norm;           /* 1: reference normalisation (Prad, 33.329), 0: plain */
+    int32_t misfit;            /* 0: -sum (D-m)^2/(E F); 1: relative; 2: trace L2    */
+    /* engine tuning: 0 = autotune */
+    int32_t steps_per_launch;  /* temporal-blocking depth T                          */
+    int32_t cols_per_lane;     /* columns per lane                                   */
+    int32_t plain;             /* 1: one solve per launch sequence, one launch per
+                                  step, no CUDA graph (the plain baseline path)      */
+} tomo_spec;
+
+typedef struct tomo_handle tomo_handle;
+
+/* optional outputs of tomo_forward; any pointer may be NULL */
+typedef struct tomo_outputs {
+    float *traces;   /* [n_cand][n_tx][n_antennas][steps]  receiver Ez traces      */
+    float *D;        /* [n_cand][n_exc][nfreq][n_angles]   far-field magnitude      */
+    float *P;        /* [n_cand][n_exc][nfreq][n_angles]   far-field phase          */
+    double *fitness; /* [n_cand] (requires a target)                                */
+    double *traces_f64; /* as traces, in double (exact copy of FP64 state)         */
+} tomo_outputs;
+
+typedef struct tomo_stats {
+    double advance_ms;        /* device time of the last batch's time loop (CUDA events)   */
+    double total_ms;          /* device time of the last batch, set-up to misfit            */
+    double cell_updates;      /* Ez cells x steps advanced in the last batch                */
+    int64_t launches;         /* advance-kernel launches in the last batch                  */
+    int64_t kernels;          /* all kernels launched in the last batch                     */
+    int32_t steps_per_launch; /* T used                                                      */
+    int32_t cols_per_lane;    /* COLS used                                                   */
+    int64_t h2d_bytes, d2h_bytes;  /* host<->device bytes of the last batch                  */
+} tomo_stats;
+
+/* ---- presets */
+/* Exactly FDTD_common.hxx: 401x401, 2000 steps, 10-cell CPML, 4 plane waves,
+   10 frequencies, 100 angles; cpu_variant selects FDTD_CPU.cxx semantics.     */
+int tomo_spec_reference(tomo_spec *spec, int cpu_variant);
+/* Breast-imaging workloads 0..4 (plain forward solve, batched PSO, precision
+   study, serving, large batch). */
+int tomo_spec_breast(tomo_spec *spec, int config);
+/* number of candidate parameters the spec expects (27, 162 or 8*n_ellipses) */
+int tomo_num_params(const tomo_spec *spec);
+/* number of excitations (solves) per candidate */
+int tomo_num_excitations(const tomo_spec *spec);
+
+/* ---- lifetime (replaces the per-call cudaMalloc/cudaFree of FDTD_GPU.cu:858-1106) */
+int tomo_create(const tomo_spec *spec, tomo_handle **out);
+void tomo_destroy(tomo_handle *h);
+/* run on this CUDA stream (cudaStream_t passed as void*); NULL = library stream */
+int tomo_set_stream(tomo_handle *h, void *stream);
+/* device-memory budget for batch and serving state, bytes (0 = 150 GB) */
+int tomo_set_memory_budget(tomo_handle *h, uint64_t bytes);
+
+/* ---- targets (the reference compiles them in: FDTD_GPU.cu:996, FDTD_CPU.cxx:789)
+   reference modes: n = n_exc*nfreq*n_angles far-field magnitudes;
+   breast mode: n = n_tx*n_antennas*steps receiver samples.                     */
+int tomo_set_target(tomo_handle *h, const float *target, size_t n);
+
+/* ---- fitness (FDTD_GPU.cu:650-1110 / FDTD_CPU.cxx:669-892)                   */
+int tomo_fitness(tomo_handle *h, const double *args, size_t n_args, double *fitness);
+/* a whole generation: args is [n_cand][n_param] row-major, fitness is [n_cand] */
+int tomo_fitness_batch(tomo_handle *h, const double *args, size_t n_cand, size_t n_param, double *fitness);
+/* forward solve with optional traces / far field / fitness */
+int tomo_forward(tomo_handle *h, const double *args, size_t n_cand, size_t n_param, const tomo_outputs *out);
+
+/* ---- serving: continuous batching of candidate requests.  There is no
+   counterpart in the reference (tao farms candidates over MPI ranks, one
+   blocking call per rank, test.cxx:82-121).  Requests are admitted in FIFO
+   order as device memory (tomo_set_memory_budget) and solve slots free up;
+   every admitted solve advances in the same kernel launches.               */
+int tomo_submit(tomo_handle *h, const double *args, size_t n_cand, size_t n_param, uint64_t *ticket);
+/* same with a per-request problem spec (e.g. another grid size; same precision) */
+int tomo_submit_spec(tomo_handle *h, const tomo_spec *spec, const double *args, size_t n_cand, size_t n_param,
+                     uint64_t *ticket);
+/* target of requests that carry `spec` (NULL = the handle's spec) */
+int tomo_set_target_spec(tomo_handle *h, const tomo_spec *spec, const float *target, size_t n);
+/* advance every admitted solve by one launch; admits queued work first          */
+int tomo_serve_step(tomo_handle *h, int *n_active);
+/* fitness of a finished ticket (n_cand values), TOMO_ENOTREADY while running    */
+int tomo_poll(tomo_handle *h, uint64_t ticket, double *fitness);
+int tomo_cancel(tomo_handle *h, uint64_t ticket);
+
+int tomo_get_stats(tomo_handle *h, tomo_stats *stats);
+const char *tomo_last_error(void);
+const char *tomo_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

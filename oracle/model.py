@@ -1,0 +1,324 @@
+"""Python side of the CPU oracle (checker only; see fdtd_oracle.h).
+
+Builds oracle problems from a spec dictionary (``Spec.as_dict()`` of the
+product, i.e. plain numbers) and runs the C restatement.  Everything derived
+from the spec -- CPML profile, material coefficients, patch / ellipse maps,
+antenna cells, source waveform, contour, far field, misfits -- is recomputed
+here or in fdtd_oracle.c from the reference formulas, independently of the
+product code.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+if HERE not in sys.path:
+    sys.path.insert(0, HERE)
+import build as _build  # noqa: E402
+
+PI = 3.141592653589793238
+MU0 = PI * 4e-7
+EPS0 = 8.85418e-12
+C0 = 1.0 / math.sqrt(MU0 * EPS0)
+ETA0 = math.sqrt(MU0 / EPS0)
+NCOEF = 8
+REF_CPML, NAN_CLAMP, PLANE_WAVE = 1, 2, 4
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_ubp = C.POINTER(C.c_ubyte)
+
+
+class OracleProblem(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int), ("ny", C.c_int), ("steps", C.c_int), ("ncpml", C.c_int),
+        ("flags", C.c_int), ("nmat", C.c_int),
+        ("dx", C.c_double), ("dt", C.c_double), ("chez", C.c_double), ("Kp", C.c_double),
+        ("cpml", _dp), ("mat", _ubp), ("mtab", _dp),
+        ("pw_kx", C.c_double), ("pw_ky", C.c_double), ("pw_xoff", C.c_double), ("pw_yoff", C.c_double),
+        ("pw_t0", C.c_double), ("pw_tau", C.c_double), ("pw_l", C.c_double), ("pw_c0", C.c_double),
+        ("src_x", C.c_int), ("src_y", C.c_int), ("src_wave", _dp),
+        ("nrx", C.c_int), ("rx", _ip), ("traces", _dp),
+        ("nf_d", C.c_int), ("nfreq", C.c_int), ("freqs", _dp), ("acc", _dp),
+        ("ez_out", _dp), ("hx_out", _dp), ("hy_out", _dp), ("jp_out", _dp),
+    ]
+
+
+_libs: dict = {}
+
+
+def lib(bits: int = 64) -> C.CDLL:
+    if bits not in _libs:
+        _build.build_oracle()
+        L = C.CDLL(_build.oracle_lib_path(bits))
+        L.oracle_solve.argtypes = [C.POINTER(OracleProblem)]
+        L.oracle_solve_many.argtypes = [C.POINTER(OracleProblem), C.c_int, C.c_int]
+        L.oracle_contour_size.argtypes = [C.c_int, C.c_int, C.c_int]
+        L.oracle_contour_point.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _ip, _ip, _ip]
+        L.oracle_far_field.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, _dp, _dp, C.c_int, C.c_int,
+                                       C.c_double, _dp, _dp]
+        L.oracle_cpml_profile.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                                          C.c_double, C.c_double, _dp]
+        L.oracle_material_coefs.argtypes = [C.c_double] * 6 + [_dp, _dp]
+        L.oracle_patch_map.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, _ubp]
+        L.oracle_ellipse_map.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, _dp, _ubp]
+        _libs[bits] = L
+    return _libs[bits]
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+# ----------------------------------------------------------------- precompute
+def cpml_profile(spec: dict) -> np.ndarray:
+    nc = spec["ncpml"]
+    out = np.zeros(6 * max(nc, 1))
+    lib().oracle_cpml_profile(nc, spec["cpml_grading"], spec["cpml_sigma_max"], spec["cpml_kappa_max"],
+                              spec["cpml_alpha_max"], spec["cpml_alpha_min"], spec["dx"], spec["dt"], _d(out))
+    return out
+
+
+def material_coefs(eps_inf: float, del_eps: float, sigma: float, spec: dict) -> tuple[np.ndarray, float]:
+    out = np.zeros(NCOEF)
+    kp = C.c_double()
+    lib().oracle_material_coefs(eps_inf, del_eps, sigma, spec["tau"], spec["dt"], spec["dx"], _d(out), C.byref(kp))
+    return out, kp.value
+
+
+def contour_size(nx: int, ny: int, d: int) -> int:
+    return lib().oracle_contour_size(nx, ny, d)
+
+
+def antenna_cells(spec: dict) -> np.ndarray:
+    n = spec["n_antennas"]
+    cells = []
+    for a in range(n):
+        th = 2 * PI * a / n
+        x = spec["nx"] / 2.0 + (spec["antenna_radius"] / spec["dx"]) * math.cos(th)
+        y = spec["ny"] / 2.0 + (spec["antenna_radius"] / spec["dx"]) * math.sin(th)
+        # C lround: half away from zero
+        cells.append((int(math.floor(x + 0.5)) if x >= 0 else -int(math.floor(-x + 0.5)),
+                      int(math.floor(y + 0.5)) if y >= 0 else -int(math.floor(-y + 0.5))))
+    return np.array(cells, dtype=np.int32)
+
+
+def source_wave(spec: dict) -> np.ndarray:
+    amp = spec["src_amp"] or (2 * spec["bg_eps_inf"] * EPS0 + spec["bg_sigma"] * spec["dt"]) / (2 * spec["dt"])
+    t = (np.arange(spec["steps"]) + 0.5) * spec["dt"] - spec["src_t0"]
+    return amp * np.sin(2 * PI * spec["src_f0"] * t) * np.exp(-(t / spec["src_tau"]) ** 2)
+
+
+def material_table_reference(args: np.ndarray, spec: dict) -> tuple[np.ndarray, float]:
+    """(nmat x NCOEF) table: material 0 vacuum, 1+p patch p (FDTD_GPU.cu:657-743 /
+    FDTD_CPU.cxx:682-698, arguments rounded to float as the reference does)."""
+    np2 = spec["npatch"] ** 2
+    a = np.asarray(args, dtype=np.float64).astype(np.float32).astype(np.float64)
+    rows, kp = [], None
+    c, kp = material_coefs(1.0, 0.0, 0.0, spec)
+    rows.append(c)
+    for p in range(np2):
+        if spec["mode"] == 0:
+            c, kp = material_coefs(a[p], a[np2 + p], a[2 * np2 + p], spec)
+        else:
+            c, kp = material_coefs(a[p], 0.0, a[np2 + p], spec)
+        rows.append(c)
+    return np.array(rows), kp
+
+
+def patch_map(spec: dict) -> np.ndarray:
+    nx, ny = spec["nx"], spec["ny"]
+    m = np.zeros((ny + 1) * (nx + 1), dtype=np.uint8)
+    lib().oracle_patch_map(nx, ny, spec["dx"], spec["breast_radius"], spec["npatch"], m.ctypes.data_as(_ubp))
+    return m
+
+
+def ellipse_geometry(params: np.ndarray) -> np.ndarray:
+    """(K, 6) = (cx, cy, a, b, cos, sin); math.cos/sin call the C library."""
+    p = np.asarray(params, dtype=np.float64).reshape(-1, 8)
+    return np.array([[e[0], e[1], e[2], e[3], math.cos(e[4]), math.sin(e[4])] for e in p]).reshape(-1, 6)
+
+
+def ellipse_map(spec: dict, params: np.ndarray) -> np.ndarray:
+    nx, ny = spec["nx"], spec["ny"]
+    geo = np.ascontiguousarray(ellipse_geometry(params))
+    m = np.zeros((ny + 1) * (nx + 1), dtype=np.uint8)
+    lib().oracle_ellipse_map(nx, ny, spec["dx"], spec["disc_radius"], geo.shape[0], _d(geo), m.ctypes.data_as(_ubp))
+    return m
+
+
+def material_table_breast(params: np.ndarray, spec: dict) -> tuple[np.ndarray, float]:
+    p = np.asarray(params, dtype=np.float64).reshape(-1, 8)
+    rows = []
+    c, kp = material_coefs(spec["bg_eps_inf"], spec["bg_del_eps"], spec["bg_sigma"], spec)
+    rows.append(c)
+    c, kp = material_coefs(spec["disc_eps_inf"], spec["disc_del_eps"], spec["disc_sigma"], spec)
+    rows.append(c)
+    for e in p:
+        c, kp = material_coefs(e[5], e[6], e[7], spec)
+        rows.append(c)
+    return np.array(rows), kp
+
+
+# ----------------------------------------------------------------- problems
+class Problem:
+    """An oracle_problem plus the numpy arrays it points into."""
+
+    def __init__(self, spec: dict, steps: int | None = None):
+        self.spec = spec
+        self.keep = []
+        self.p = OracleProblem()
+        p = self.p
+        p.nx, p.ny = spec["nx"], spec["ny"]
+        p.steps = spec["steps"] if steps is None else steps
+        p.ncpml = spec["ncpml"]
+        p.dx, p.dt = spec["dx"], spec["dt"]
+        p.chez = (spec["dt"] / spec["dx"]) / MU0
+        p.src_x = p.src_y = -1
+        self._arr("cpml", cpml_profile(spec))
+
+    def _arr(self, field: str, a: np.ndarray, ctype=_dp):
+        a = np.ascontiguousarray(a)
+        self.keep.append(a)
+        setattr(self.p, field, a.ctypes.data_as(ctype))
+        return a
+
+    def set_materials(self, mat: np.ndarray, tab: np.ndarray, kp: float):
+        self.mat = self._arr("mat", mat.astype(np.uint8), _ubp)
+        self.p.nmat = tab.shape[0]
+        self._arr("mtab", tab.astype(np.float64))
+        self.p.Kp = kp
+
+    def want_traces(self, rx: np.ndarray):
+        self.p.nrx = rx.shape[0]
+        self._arr("rx", rx.astype(np.int32).ravel(), _ip)
+        self.traces = self._arr("traces", np.zeros((rx.shape[0], self.p.steps)))
+
+    def want_dft(self, d: int, freqs):
+        self.p.nf_d = d
+        self.p.nfreq = len(freqs)
+        self._arr("freqs", np.array(freqs, dtype=np.float64))
+        C_ = contour_size(self.p.nx, self.p.ny, d)
+        self.acc = self._arr("acc", np.zeros((len(freqs), C_, 4)))
+
+    def want_fields(self):
+        nx, ny = self.p.nx, self.p.ny
+        self.ez = self._arr("ez_out", np.zeros((ny + 1, nx + 1)))
+        self.jp = self._arr("jp_out", np.zeros((ny + 1, nx + 1)))
+        self.hx = self._arr("hx_out", np.zeros((ny, nx)))
+        self.hy = self._arr("hy_out", np.zeros((ny, nx)))
+
+
+def reference_problem(spec: dict, args: np.ndarray, exc: int, steps: int | None = None) -> Problem:
+    """One plane-wave excitation of the reference modes (FDTD_GPU.cu:937-985 /
+    FDTD_CPU.cxx:799-840)."""
+    pr = Problem(spec, steps)
+    tab, kp = material_table_reference(args, spec)
+    pr.set_materials(patch_map(spec), tab, kp)
+    p = pr.p
+    p.flags = REF_CPML | PLANE_WAVE | (NAN_CLAMP if spec["nan_clamp"] else 0)
+    phi = float(np.float32(exc * 2 * PI / spec["n_excitations"]))
+    p.pw_kx, p.pw_ky = math.cos(phi), math.sin(phi)
+    off = spec["nx"] // 2 if spec["pw_centred"] else 0
+    p.pw_xoff = p.pw_yoff = float(off)
+    p.pw_t0, p.pw_tau, p.pw_l, p.pw_c0 = spec["pw_t0"], spec["pw_tau"], spec["pw_l"], C0
+    if spec["nfreq"] > 0:
+        pr.want_dft(spec["nf2ff_d"], spec["freqs"])
+    return pr
+
+
+def breast_problem(spec: dict, params: np.ndarray, tx: int, steps: int | None = None) -> Problem:
+    """One transmitter of the breast-imaging mode."""
+    pr = Problem(spec, steps)
+    tab, kp = material_table_breast(params, spec)
+    pr.set_materials(ellipse_map(spec, params), tab, kp)
+    ant = antenna_cells(spec)
+    p = pr.p
+    p.flags = 0
+    p.src_x, p.src_y = int(ant[tx, 0]), int(ant[tx, 1])
+    pr._arr("src_wave", source_wave(spec)[: p.steps].copy())
+    pr.want_traces(ant)
+    if spec["nfreq"] > 0:
+        pr.want_dft(spec["nf2ff_d"], spec["freqs"])
+    return pr
+
+
+def run(problems: list, bits: int = 64, threads: int | None = None) -> None:
+    arr = (OracleProblem * len(problems))(*[pr.p for pr in problems])
+    n = threads or min(len(problems), os.cpu_count() or 1)
+    rc = lib(bits).oracle_solve_many(arr, len(problems), n)
+    if rc != 0:
+        raise RuntimeError("oracle_solve_many failed")
+
+
+def far_field(pr: Problem, norm: int, tau: float, nangle: int, bits: int = 64) -> tuple[np.ndarray, np.ndarray]:
+    s = pr.spec
+    F = pr.p.nfreq
+    D = np.zeros((F, nangle))
+    P = np.zeros((F, nangle))
+    freqs = np.array(s["freqs"][:F], dtype=np.float64)
+    lib(bits).oracle_far_field(pr.p.nx, pr.p.ny, pr.p.nf_d, pr.p.dx, F, _d(freqs), _d(pr.acc), nangle, norm, tau,
+                               _d(D), _d(P))
+    return D, P
+
+
+# ----------------------------------------------------------------- misfits
+def misfit_abs(D: np.ndarray, m: np.ndarray, n_exc: int, nfreq: int) -> float:
+    """FDTD_GPU.cu:1004-1022: -sum (D - m)^2 / (E F)."""
+    D = np.asarray(D, dtype=np.float64).ravel()
+    m = np.asarray(m, dtype=np.float64).ravel()[: D.size]
+    return float(-np.sum((D - m) ** 2 / (n_exc * nfreq)))
+
+
+def misfit_rel(D: np.ndarray, m: np.ndarray, n_exc: int, nfreq: int) -> float:
+    """FDTD_CPU.cxx:841-845: -sum (D - m)^2 / (m^2 E F)."""
+    D = np.asarray(D, dtype=np.float64).ravel()
+    m = np.asarray(m, dtype=np.float64).ravel()[: D.size]
+    return float(-np.sum((D - m) ** 2 / (m * m * n_exc * nfreq)))
+
+
+def misfit_trace(traces: np.ndarray, target: np.ndarray) -> float:
+    """-sum (s - t)^2 / sum t^2 over transmitters, receivers and steps."""
+    s = np.asarray(traces, dtype=np.float64).ravel()
+    t = np.asarray(target, dtype=np.float64).ravel()
+    return float(-np.sum((s - t) ** 2) / np.sum(t * t))
+
+
+# ----------------------------------------------------------------- whole evaluations
+def reference_forward(spec: dict, args: np.ndarray, steps: int | None = None, bits: int = 64,
+                      fields: bool = False) -> dict:
+    """All excitations of one reference-mode candidate: D, P [E][F][A] and DFT accumulators."""
+    E = spec["n_excitations"]
+    probs = [reference_problem(spec, args, e, steps) for e in range(E)]
+    if fields:
+        for pr in probs:
+            pr.want_fields()
+    run(probs, bits)
+    D = np.zeros((E, spec["nfreq"], spec["n_angles"]))
+    P = np.zeros_like(D)
+    for e, pr in enumerate(probs):
+        D[e], P[e] = far_field(pr, spec["ff_norm"], spec["pw_tau"], spec["n_angles"], bits)
+    return {"D": D, "P": P, "problems": probs}
+
+
+def breast_forward(spec: dict, params: np.ndarray, steps: int | None = None, bits: int = 64,
+                   txs=None, fields: bool = False) -> dict:
+    txs = list(range(spec["n_tx"])) if txs is None else list(txs)
+    probs = [breast_problem(spec, params, t, steps) for t in txs]
+    if fields:
+        for pr in probs:
+            pr.want_fields()
+    run(probs, bits)
+    out = {"traces": np.stack([pr.traces for pr in probs]), "problems": probs}
+    if spec["nfreq"] > 0:
+        DP = [far_field(pr, spec["ff_norm"], spec["pw_tau"], spec["n_angles"], bits) for pr in probs]
+        out["D"] = np.stack([d for d, _ in DP])
+        out["P"] = np.stack([p for _, p in DP])
+    return out

@@ -1,0 +1,90 @@
+"""GPU path in the reference's own modes, against the reference itself.
+
+* FDTD_CPU semantics (9x9 patches, uncentred plane wave, relative misfit) vs
+  golden vectors produced by the reference's own CPU code (tests/golden/):
+  far-field magnitudes D after 1000 steps and the full-size fitness of
+  FDTD_CPU(args) (401x401, 2000 steps).  Tolerances: D max error <= 1e-4 of
+  max |D| (the FP32 reference and the FP32 GPU path round differently);
+  fitness relative error <= 1e-3 (the reference accumulates the misfit in
+  float over 4000 terms).
+* FDTD_GPU semantics (3x3 Debye patches, centred plane wave) at full size,
+  FP64 GPU vs FP64 oracle: D rel-L2 <= 1e-5 (D leaves the device as float),
+  fitness relative error <= 1e-6.
+* The drop-in FDTD_GPU(arguments) entry point.
+"""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+import pytest
+
+from helpers import rel_l2
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _golden(name):
+    path = os.path.join(GOLD, f"ref_cpu_{name}.npz")
+    if not os.path.exists(path):
+        pytest.skip("golden fixture missing")
+    return np.load(path)
+
+
+@pytest.mark.parametrize("case", ["dielectric", "random", "vacuum"])
+def test_cpu_semantics_far_field_vs_reference(tomo, case):
+    g = _golden(case)
+    spec = tomo.reference_spec(True).copy(steps=int(g["steps"]))
+    with tomo.Solver(spec) as s:
+        out = s.forward(g["args"], traces=False, far_field=True)
+    D = out["D"][0]
+    Dref = g["D"].astype(np.float64)
+    scale = max(np.abs(Dref).max(), 1e-30)
+    assert np.abs(D - Dref).max() <= 1e-4 * scale if scale > 1e-30 else np.abs(D).max() == 0.0
+
+
+@pytest.mark.parametrize("case", ["dielectric", "random", "vacuum"])
+def test_cpu_semantics_fitness_vs_reference(tomo, case):
+    g = _golden(case)
+    if "fitness_full" not in g:
+        pytest.skip("no full-size fitness in fixture")
+    meas = np.load(os.path.join(GOLD, "ref_measurement_cpu.npy"))
+    with tomo.Solver(tomo.reference_spec(True)) as s:
+        s.set_target(meas)
+        fit = s.fitness(g["args"])
+    want = float(g["fitness_full"])
+    assert abs(fit - want) <= 1e-3 * abs(want), (fit, want)
+
+
+def test_gpu_semantics_full_size_fp64_vs_oracle(tomo, oracle):
+    from tomography_gb300 import workloads as W
+
+    args = W.reference_patch_args(4242)
+    meas = np.load(os.path.join(GOLD, "ref_measurement_gpu.npy"))[:4000]
+    spec = tomo.reference_spec(False).copy(precision=tomo.FP64, steps_per_launch=1, cols_per_lane=1)
+    with tomo.Solver(spec) as s:
+        s.set_target(meas)
+        out = s.forward(args, traces=False, far_field=True, fitness=True)
+    ref = oracle.reference_forward(spec.as_dict(), args)
+    assert rel_l2(out["D"][0], ref["D"]) <= 1e-5
+    want = oracle.misfit_abs(ref["D"].astype(np.float32), meas, 4, 10)
+    assert abs(out["fitness"][0] - want) <= 1e-6 * abs(want), (out["fitness"][0], want)
+
+
+def test_dropin_fdtd_gpu(tomo):
+    from tomography_gb300 import workloads as W
+
+    meas = np.load(os.path.join(GOLD, "ref_measurement_gpu.npy"))
+    args = list(W.reference_patch_args(7))
+    fit = tomo.FDTD_GPU(args, measurement=meas)
+    assert np.isfinite(fit) and fit <= 0
+    with tomo.Solver(tomo.reference_spec(False)) as s:
+        s.set_target(meas[:4000])
+        assert s.fitness(args) == fit
+    with pytest.raises(IndexError):
+        tomo.FDTD_GPU(args[:20])
+    # vacuum: D == 0, so the fitness is -sum(m^2)/40 exactly
+    vac = [1.0] * 9 + [0.0] * 18
+    want = -float(np.sum(meas[:4000].astype(np.float64) ** 2)) / 40.0
+    assert abs(tomo.FDTD_GPU(vac) - want) <= 1e-12 * abs(want)

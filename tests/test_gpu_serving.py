@@ -1,0 +1,110 @@
+"""Serving loop: continuous batching with admission by memory budget.
+
+The same request must give bit-identical fitness alone, in a mix with other
+requests (admitted while it runs, different progress), and through the
+batch path (same kernels, same blocking).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from helpers import small_breast_spec, small_params
+
+pytestmark = pytest.mark.gpu
+
+
+def _cands(W, n, seed, k=4):
+    return np.stack([W.candidate_params(seed + 1000 * i, k, disc_radius=15e-3) for i in range(n)])
+
+
+def _drain(solver, tickets, ncands, max_steps=100000):
+    done = {}
+    for _ in range(max_steps):
+        solver.serve_step()
+        for t, n in zip(tickets, ncands):
+            if t not in done:
+                r = solver.poll(t, n)
+                if r is not None:
+                    done[t] = r
+        if len(done) == len(tickets):
+            return done
+    raise AssertionError("serving loop did not finish")
+
+
+def _solver(tomo, W, **kw):
+    spec = small_breast_spec(tomo, n_ellipses=4, steps=240, **kw)
+    s = tomo.Solver(spec)
+    tgt = s.forward(small_params(W, 4), traces=True, far_field=False)["traces"][0]
+    s.set_target(tgt)
+    return s
+
+
+def test_alone_equals_mix_equals_batch(tomo):
+    from tomography_gb300 import workloads as W
+
+    A = _cands(W, 2, 111)
+    B = _cands(W, 3, 222)
+    C = _cands(W, 1, 333)
+    with _solver(tomo, W) as s:
+        batch = s.fitness_batch(A)
+        ta = s.submit(A)
+        alone = _drain(s, [ta], [2])[ta]
+        # mix: B starts first, A joins while B runs, C joins later
+        tb = s.submit(B)
+        for _ in range(5):
+            s.serve_step()
+        ta2 = s.submit(A)
+        for _ in range(3):
+            s.serve_step()
+        tc = s.submit(C)
+        res = _drain(s, [tb, ta2, tc], [3, 2, 1])
+        np.testing.assert_array_equal(alone, batch)
+        np.testing.assert_array_equal(res[ta2], alone)
+        np.testing.assert_array_equal(res[tb], s.fitness_batch(B))
+        np.testing.assert_array_equal(res[tc], s.fitness_batch(C))
+
+
+def test_mixed_grid_sizes_in_one_launch(tomo):
+    from tomography_gb300 import workloads as W
+
+    A = _cands(W, 2, 444)
+    with _solver(tomo, W) as s:
+        big = small_breast_spec(tomo, n_ellipses=4, steps=240, nx=128, ny=128)
+        with tomo.Solver(big) as ref_solver:
+            tgt = ref_solver.forward(small_params(W, 4), traces=True, far_field=False)["traces"][0]
+            ref_solver.set_target(tgt)
+            want_big = ref_solver.fitness_batch(A)
+        s.set_target_for(big, tgt)
+        want_small = s.fitness_batch(A)
+        t1 = s.submit(A)
+        t2 = s.submit(A, spec=big)
+        res = _drain(s, [t1, t2], [2, 2])
+        np.testing.assert_array_equal(res[t1], want_small)
+        np.testing.assert_array_equal(res[t2], want_big)
+
+
+def test_budget_admission_and_cancel(tomo):
+    from tomography_gb300 import workloads as W
+
+    A = _cands(W, 2, 555)
+    with _solver(tomo, W) as s:
+        want = s.fitness_batch(A)
+        # a budget for about one request: the second waits, then runs
+        s.set_memory_budget(1)
+        with pytest.raises(tomo.TomoError) as ei:
+            t = s.submit(A)
+            s.serve_step()
+        assert ei.value.status == -2   # TOMO_ENOMEM_BUDGET for a request above the budget
+        s.set_memory_budget(0)
+        t1 = s.submit(A)
+        t2 = s.submit(A)
+        t3 = s.submit(A)
+        s.serve_step()
+        s.cancel(t2)
+        res = _drain(s, [t1, t3], [2, 2])
+        np.testing.assert_array_equal(res[t1], want)
+        np.testing.assert_array_equal(res[t3], want)
+        with pytest.raises(tomo.TomoError) as ei:
+            s.poll(t2, 2)
+        assert ei.value.status == -7   # TOMO_ECANCELLED

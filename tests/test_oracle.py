@@ -1,0 +1,172 @@
+"""CPU: the oracle (C restatement) pinned against the reference's own CPU code.
+
+The golden fixtures were produced by the reference's FDTD_CPU.cxx functions
+(tests/golden/make_golden.py).  The oracle in FP64 must reproduce them to
+FP32 accuracy: the reference computes in float, so fields / probe traces agree
+to rel-L2 <= 1e-5 and far-field D to max error <= 1e-5 of max |D| after 1000
+steps (measured: ~3e-6 and ~2e-6).
+"""
+from __future__ import annotations
+
+import math
+import os
+
+import numpy as np
+import pytest
+
+from helpers import rel_l2
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+PI = 3.141592653589793238
+
+
+def reference_cpu_spec() -> dict:
+    """FDTD_common.hxx:3-59 with the FDTD_CPU.cxx semantics, as plain numbers
+    (independent of the product's preset function)."""
+    br, dx = 0.0315, 0.001
+    mu0, eps0 = PI * 4e-7, 8.85418e-12
+    c0 = 1 / math.sqrt(mu0 * eps0)
+    tau = 3.3445267e-11
+    return dict(mode=1, nx=401, ny=401, dx=dx, dt=dx / c0 / 2, steps=2000, ncpml=10, cpml_grading=2.0,
+                cpml_sigma_max=3 / (150 * PI * dx), cpml_kappa_max=10.0, cpml_alpha_max=0.01, cpml_alpha_min=0.0,
+                tau=7e-12, breast_radius=br, npatch=9, n_excitations=4, pw_tau=tau, pw_t0=math.sqrt(20) * tau,
+                pw_l=-br, pw_centred=0, nan_clamp=0, nf2ff_d=100, nfreq=10,
+                freqs=[1e9 + 1e9 * k for k in range(10)], n_angles=100, ff_norm=1, misfit=1)
+
+
+def _golden(name):
+    path = os.path.join(GOLD, f"ref_cpu_{name}.npz")
+    if not os.path.exists(path):
+        pytest.skip("golden fixture missing")
+    return np.load(path)
+
+
+def test_product_preset_equals_reference_constants(tomo):
+    s = tomo.reference_spec(True).as_dict()
+    want = reference_cpu_spec()
+    for k, v in want.items():
+        if isinstance(v, list):
+            assert np.allclose(s[k], v, rtol=1e-15), k
+        else:
+            assert s[k] == pytest.approx(v, rel=1e-15, abs=0), k
+    assert s["nx"] == 401 and s["nf2ff_d"] == 100
+
+
+@pytest.mark.parametrize("case", ["dielectric", "random"])
+def test_oracle_fp64_vs_reference_cpu(oracle, case):
+    g = _golden(case)
+    spec = reference_cpu_spec()
+    steps = int(g["steps"])
+    probs = [oracle.reference_problem(spec, g["args"], e, steps) for e in range(4)]
+    for pr in probs:
+        pr.want_traces(g["probe_xy"])
+    probs[0].want_fields()
+    oracle.run(probs, 64)
+    # probe traces of every excitation
+    tr = np.stack([pr.traces.T for pr in probs])            # [E][steps][probe]
+    assert rel_l2(tr, g["traces"]) <= 1e-5
+    # final fields of excitation 0 on the breast window and a coarse sample
+    lo, hi = g["win"]
+    assert rel_l2(probs[0].ez[lo:hi, lo:hi], g["Ez_win"]) <= 1e-5
+    assert rel_l2(probs[0].hx[lo:hi, lo:hi], g["Hx_win"]) <= 1e-5
+    assert rel_l2(probs[0].hy[lo:hi, lo:hi], g["Hy_win"]) <= 1e-5
+    assert rel_l2(probs[0].ez[::8, ::8], g["Ez_sub8"]) <= 1e-5
+    # running-DFT surface currents: reference face arrays -> contour order
+    nx, d = 401, 100
+    l1 = nx - 2 * d - 2
+    for e in (0, 2):
+        acc = probs[e].acc                                    # [F][C][4]
+        for fi, f in enumerate(g["acc_freqs"]):
+            a = acc[f]
+            J = a[:, 0] + 1j * a[:, 1]
+            M = a[:, 2] + 1j * a[:, 3]
+            # face order in the contour: yn [0,l1), xp [l1,l2), yp [l2,l3), xn [l3,C)
+            l2, l3 = l1 + (nx - 2 * d), 2 * l1 + (nx - 2 * d)
+            ref = {k: g[f"{k}_e{e}"][fi][:, 0] + 1j * g[f"{k}_e{e}"][fi][:, 1]
+                   for k in ("cjzyn", "cjzxp", "cjzyp", "cjzxn", "cmxyn", "cmyxp", "cmxyp", "cmyxn")}
+            gotJ = np.concatenate([J[:l1], J[l1:l2], J[l2:l3], J[l3:]])
+            refJ = np.concatenate([ref["cjzyn"], ref["cjzxp"], ref["cjzyp"], ref["cjzxn"]])
+            gotM = np.concatenate([M[:l1], M[l1:l2], M[l2:l3], M[l3:]])
+            refM = np.concatenate([ref["cmxyn"], ref["cmyxp"], ref["cmxyp"], ref["cmyxn"]])
+            assert rel_l2(gotJ, refJ) <= 1e-4, (e, f)
+            assert rel_l2(gotM, refM) <= 1e-4, (e, f)
+    # far field
+    D = np.stack([oracle.far_field(pr, 1, spec["pw_tau"], 100)[0] for pr in probs])
+    Dref = g["D"].astype(np.float64)
+    assert np.abs(D - Dref).max() <= 1e-5 * np.abs(Dref).max()
+
+
+def test_oracle_vacuum_is_exactly_zero(oracle):
+    g = _golden("vacuum")
+    spec = reference_cpu_spec()
+    out = oracle.reference_forward(spec, g["args"], steps=200)
+    assert np.all(out["D"] == 0.0)
+    assert np.all(g["D"] == 0.0)
+    meas = np.load(os.path.join(GOLD, "ref_measurement_cpu.npy"))
+    # D == 0: relative misfit is exactly -4000/40
+    assert oracle.misfit_rel(np.zeros(4000), meas, 4, 10) == pytest.approx(-100.0, rel=1e-14)
+
+
+def test_reference_full_fitness_fixtures():
+    """The reference's own full-size fitness values, as recorded in the fixtures."""
+    for case, want in (("vacuum", -100.0038), ("dielectric", -48249.9)):
+        g = _golden(case)
+        if "fitness_full" not in g:
+            pytest.skip("no full-size fitness in fixture")
+        assert float(g["fitness_full"]) == pytest.approx(want, rel=1e-5)
+
+
+def test_contour_matches_reference_index_maps(oracle):
+    """FDTD_common.cxx:4-46: 800 points, faces of 199/201/199/201 on the
+    reference grid, face order yn, xp, yp, xn, corners on the x faces."""
+    import ctypes as C
+
+    nx = ny = 401
+    d = 100
+    n = oracle.contour_size(nx, ny, d)
+    assert n == 800
+    faces = []
+    for i in range(n):
+        x, y, f = C.c_int(), C.c_int(), C.c_int()
+        oracle.lib().oracle_contour_point(nx, ny, d, i, C.byref(x), C.byref(y), C.byref(f))
+        faces.append((x.value, y.value, f.value))
+    counts = np.bincount([f for _, _, f in faces])
+    assert list(counts) == [199, 201, 199, 201]
+    assert faces[0] == (101, 100, 0) and faces[198] == (299, 100, 0)
+    assert faces[199] == (300, 100, 1) and faces[399] == (300, 300, 1)
+    assert faces[400] == (299, 300, 2) and faces[598] == (101, 300, 2)
+    assert faces[599] == (100, 300, 3) and faces[799] == (100, 100, 3)
+    assert len(set((x, y) for x, y, _ in faces)) == 800
+
+
+def test_patch_maps(oracle):
+    spec = reference_cpu_spec()
+    m9 = oracle.patch_map(spec)
+    # corner patches of the 9x9 lattice lie outside the disc
+    assert m9.max() <= 81 and set(np.unique(m9)) <= set(range(82)) and len(np.unique(m9)) > 60
+    spec3 = dict(spec, npatch=3)
+    m3 = oracle.patch_map(spec3)
+    assert set(np.unique(m3)) == set(range(10))
+    # breast disc of radius 31.5 cells about (200, 200)
+    inside = (m3.reshape(402, 402) > 0)
+    j, i = np.nonzero(inside)
+    assert inside.sum() == np.sum(((np.arange(402)[None, :] - 200) ** 2 +
+                                   (np.arange(402)[:, None] - 200) ** 2) <= 31.5 ** 2)
+    assert i.min() == 169 and i.max() == 231 and j.min() == 169 and j.max() == 231
+
+
+def test_material_coefficients_match_reference_formulas(oracle):
+    """FDTD_GPU.cu:739-741, 1118-1120 for one Debye material."""
+    spec = reference_cpu_spec()
+    einf, deps, sig = 3.14, 1.61, 0.02
+    dt, dx, tau, eps0 = spec["dt"], spec["dx"], spec["tau"], 8.85418e-12
+    c, kp = oracle.material_coefs(einf, deps, sig, spec)
+    beta = eps0 * deps * dt / (tau * (1 + dt / (2 * tau)))
+    den = 2 * einf * eps0 + sig * dt + beta
+    assert kp == pytest.approx((1 - dt / (2 * tau)) / (1 + dt / (2 * tau)), rel=1e-15)
+    assert c[0] == pytest.approx((2 * einf * eps0 - sig * dt + beta) / den, rel=1e-15)
+    assert c[1] == pytest.approx((2 * dt / dx) / den, rel=1e-15)
+    assert c[2] == pytest.approx((1 + kp) * dt / den, rel=1e-15)
+    assert c[3] == pytest.approx(beta / dt, rel=1e-15)
+    assert c[4] == pytest.approx((-2 * eps0 * einf + 2 * eps0 - sig * dt - beta) / den, rel=1e-15)
+    assert c[5] == pytest.approx((2 * eps0 * einf - 2 * eps0 - sig * dt + beta) / den, rel=1e-15)

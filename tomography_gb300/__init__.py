@@ -1,0 +1,302 @@
+"""tomography_gb300: GB300-native forward FDTD fitness path for microwave tomography.
+
+Python mirror of the reference's operator interface.  The reference exposes
+``double FDTD_GPU(const std::vector<double>&)`` (FDTD_GPU.cuh:8) and tao's
+search drivers call it once per candidate (test.cxx:94-121).  Here the same
+entry point is :func:`FDTD_GPU`, and the batched / serving interfaces of the
+native library are exposed through :class:`Solver`.  Everything runs in the
+native library ``_lib/libtomography_gb300.so`` (hand-written sm_103a CUDA
+kernels behind the C ABI of ``include/tomography.h``); there is no Python or
+CPU fallback: if the library cannot be loaded, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+from .spec import Spec, MODE_REFERENCE_GPU, MODE_REFERENCE_CPU, MODE_BREAST, FP32, FP64, MAX_FREQS  # noqa: F401
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libtomography_gb300.so")
+
+TOMO_OK = 0
+STATUS_NAMES = {
+    -1: "TOMO_EINVAL",
+    -2: "TOMO_ENOMEM_BUDGET",
+    -3: "TOMO_ETIMEOUT",
+    -4: "TOMO_ENUMERIC",
+    -5: "TOMO_ECUDA",
+    -6: "TOMO_ENOTREADY",
+    -7: "TOMO_ECANCELLED",
+    -8: "TOMO_ENOTARGET",
+}
+
+
+class TomoError(RuntimeError):
+    """A non-OK status from the native library."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class Outputs(C.Structure):
+    _fields_ = [
+        ("traces", C.POINTER(C.c_float)),
+        ("D", C.POINTER(C.c_float)),
+        ("P", C.POINTER(C.c_float)),
+        ("fitness", C.POINTER(C.c_double)),
+        ("traces_f64", C.POINTER(C.c_double)),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("advance_ms", C.c_double),
+        ("total_ms", C.c_double),
+        ("cell_updates", C.c_double),
+        ("launches", C.c_int64),
+        ("kernels", C.c_int64),
+        ("steps_per_launch", C.c_int32),
+        ("cols_per_lane", C.c_int32),
+        ("h2d_bytes", C.c_int64),
+        ("d2h_bytes", C.c_int64),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+_lib: Optional[C.CDLL] = None
+
+
+def library() -> C.CDLL:
+    """Load the native library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"native library missing: {LIB_PATH} (run __graft_entry__.build())")
+    lib = C.CDLL(LIB_PATH)
+    P, I, SZ = C.c_void_p, C.c_int, C.c_size_t
+    dp, fp = C.POINTER(C.c_double), C.POINTER(C.c_float)
+    sig = {
+        "tomo_spec_reference": (I, [C.POINTER(Spec), I]),
+        "tomo_spec_breast": (I, [C.POINTER(Spec), I]),
+        "tomo_num_params": (I, [C.POINTER(Spec)]),
+        "tomo_num_excitations": (I, [C.POINTER(Spec)]),
+        "tomo_create": (I, [C.POINTER(Spec), C.POINTER(P)]),
+        "tomo_destroy": (None, [P]),
+        "tomo_set_stream": (I, [P, P]),
+        "tomo_set_memory_budget": (I, [P, C.c_uint64]),
+        "tomo_set_target": (I, [P, fp, SZ]),
+        "tomo_fitness": (I, [P, dp, SZ, dp]),
+        "tomo_fitness_batch": (I, [P, dp, SZ, SZ, dp]),
+        "tomo_forward": (I, [P, dp, SZ, SZ, C.POINTER(Outputs)]),
+        "tomo_submit": (I, [P, dp, SZ, SZ, C.POINTER(C.c_uint64)]),
+        "tomo_submit_spec": (I, [P, C.POINTER(Spec), dp, SZ, SZ, C.POINTER(C.c_uint64)]),
+        "tomo_set_target_spec": (I, [P, C.POINTER(Spec), fp, SZ]),
+        "tomo_serve_step": (I, [P, C.POINTER(C.c_int)]),
+        "tomo_poll": (I, [P, C.c_uint64, dp]),
+        "tomo_cancel": (I, [P, C.c_uint64]),
+        "tomo_get_stats": (I, [P, C.POINTER(Stats)]),
+        "tomo_last_error": (C.c_char_p, []),
+        "tomo_version": (C.c_char_p, []),
+        "tomo_fdtd_gpu_set_target": (I, [fp, SZ]),
+        "tomo_fdtd_gpu_release": (None, []),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _check(rc: int) -> None:
+    if rc != TOMO_OK:
+        raise TomoError(rc, library().tomo_last_error().decode())
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _fptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def reference_spec(cpu_variant: bool = False) -> Spec:
+    """The reference's compile-time problem (FDTD_common.hxx:1-76) as a runtime spec."""
+    s = Spec()
+    _check(library().tomo_spec_reference(C.byref(s), 1 if cpu_variant else 0))
+    return s
+
+
+def breast_spec(config: int) -> Spec:
+    """Breast-imaging workload presets 0..4."""
+    s = Spec()
+    _check(library().tomo_spec_breast(C.byref(s), int(config)))
+    return s
+
+
+class Solver:
+    """One device-resident solver instance (C handle) for one problem spec."""
+
+    def __init__(self, spec: Spec, stream: Optional[int] = None):
+        lib = library()
+        self.spec = Spec()
+        C.memmove(C.byref(self.spec), C.byref(spec), C.sizeof(Spec))
+        h = C.c_void_p()
+        _check(lib.tomo_create(C.byref(self.spec), C.byref(h)))
+        self._h = h
+        self.n_params = lib.tomo_num_params(C.byref(self.spec))
+        self.n_exc = lib.tomo_num_excitations(C.byref(self.spec))
+        if stream is not None:
+            self.set_stream(stream)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            library().tomo_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- configuration
+    def set_stream(self, stream: int) -> None:
+        _check(library().tomo_set_stream(self._h, C.c_void_p(stream)))
+
+    def set_memory_budget(self, nbytes: int) -> None:
+        _check(library().tomo_set_memory_budget(self._h, C.c_uint64(int(nbytes))))
+
+    def set_target(self, target: np.ndarray) -> None:
+        t = np.ascontiguousarray(target, dtype=np.float32).ravel()
+        _check(library().tomo_set_target(self._h, _fptr(t), t.size))
+
+    # -- evaluation
+    def _args(self, args) -> np.ndarray:
+        a = np.ascontiguousarray(args, dtype=np.float64)
+        if a.ndim == 1:
+            a = a[None, :]
+        if a.shape[1] != self.n_params:
+            raise ValueError(f"expected {self.n_params} parameters per candidate, got {a.shape[1]}")
+        return a
+
+    def fitness(self, args: Sequence[float]) -> float:
+        a = self._args(args)
+        out = np.zeros(1, dtype=np.float64)
+        _check(library().tomo_fitness(self._h, _dptr(a), a.shape[1], _dptr(out)))
+        return float(out[0])
+
+    def fitness_batch(self, args, out: Optional[np.ndarray] = None) -> np.ndarray:
+        a = self._args(args)
+        if out is None:
+            out = np.zeros(a.shape[0], dtype=np.float64)
+        _check(library().tomo_fitness_batch(self._h, _dptr(a), a.shape[0], a.shape[1], _dptr(out)))
+        return out
+
+    def forward(self, args, traces: bool = True, far_field: bool = True, fitness: bool = False,
+                traces_f64: bool = False) -> dict:
+        """Forward solves of a batch; returns numpy arrays of the requested outputs."""
+        a = self._args(args)
+        n = a.shape[0]
+        s = self.spec
+        res: dict = {}
+        o = Outputs()
+        if traces and s.mode == MODE_BREAST:
+            res["traces"] = np.zeros((n, self.n_exc, s.n_antennas, s.steps), dtype=np.float32)
+            o.traces = _fptr(res["traces"])
+        if traces_f64 and s.mode == MODE_BREAST:
+            res["traces_f64"] = np.zeros((n, self.n_exc, s.n_antennas, s.steps), dtype=np.float64)
+            o.traces_f64 = _dptr(res["traces_f64"])
+        if far_field and s.nfreq > 0:
+            res["D"] = np.zeros((n, self.n_exc, s.nfreq, s.n_angles), dtype=np.float32)
+            res["P"] = np.zeros_like(res["D"])
+            o.D = _fptr(res["D"])
+            o.P = _fptr(res["P"])
+        if fitness:
+            res["fitness"] = np.zeros(n, dtype=np.float64)
+            o.fitness = _dptr(res["fitness"])
+        _check(library().tomo_forward(self._h, _dptr(a), n, a.shape[1], C.byref(o)))
+        return res
+
+    # -- serving
+    def submit(self, args, spec: Optional[Spec] = None) -> int:
+        """Queue a request; ``spec`` may select another grid (same precision)."""
+        a = np.ascontiguousarray(args, dtype=np.float64)
+        if a.ndim == 1:
+            a = a[None, :]
+        t = C.c_uint64()
+        if spec is None:
+            a = self._args(a)
+            _check(library().tomo_submit(self._h, _dptr(a), a.shape[0], a.shape[1], C.byref(t)))
+        else:
+            _check(library().tomo_submit_spec(self._h, C.byref(spec), _dptr(a), a.shape[0], a.shape[1], C.byref(t)))
+        return int(t.value)
+
+    def set_target_for(self, spec: Spec, target: np.ndarray) -> None:
+        t = np.ascontiguousarray(target, dtype=np.float32).ravel()
+        _check(library().tomo_set_target_spec(self._h, C.byref(spec), _fptr(t), t.size))
+
+    def serve_step(self) -> int:
+        n = C.c_int()
+        _check(library().tomo_serve_step(self._h, C.byref(n)))
+        return int(n.value)
+
+    def poll(self, ticket: int, n_cand: int) -> Optional[np.ndarray]:
+        out = np.zeros(n_cand, dtype=np.float64)
+        rc = library().tomo_poll(self._h, C.c_uint64(ticket), _dptr(out))
+        if rc == -6:
+            return None
+        _check(rc)
+        return out
+
+    def cancel(self, ticket: int) -> None:
+        _check(library().tomo_cancel(self._h, C.c_uint64(ticket)))
+
+    def stats(self) -> dict:
+        st = Stats()
+        _check(library().tomo_get_stats(self._h, C.byref(st)))
+        return st.as_dict()
+
+
+_dropin: Optional[Solver] = None
+
+
+def FDTD_GPU(arguments: Sequence[float], measurement: Optional[np.ndarray] = None) -> float:
+    """Drop-in for ``double FDTD_GPU(const std::vector<double>&)`` (FDTD_GPU.cuh:8).
+
+    ``arguments``: 27 values, eps_inf of the 3x3 patches, then del_eps, then
+    sigma (FDTD_GPU.cu:657-693).  Raises IndexError for a short vector (the
+    reference's ``.at()`` throws std::out_of_range).  The far-field target is
+    ``measurement`` (first call) or the file named by TOMO_MEASUREMENT_FILE.
+    """
+    global _dropin
+    args = [float(v) for v in arguments]
+    if len(args) < 27:
+        raise IndexError("FDTD_GPU: expected 27 arguments")
+    if _dropin is None:
+        solver = Solver(reference_spec(False))
+        if measurement is None:
+            path = os.environ.get("TOMO_MEASUREMENT_FILE")
+            if not path:
+                raise TomoError(-8, "no target: pass measurement= or set TOMO_MEASUREMENT_FILE")
+            measurement = np.fromfile(path, dtype=np.float32)
+        solver.set_target(np.asarray(measurement, dtype=np.float32)[:4000])
+        _dropin = solver
+    elif measurement is not None:
+        _dropin.set_target(np.asarray(measurement, dtype=np.float32)[:4000])
+    return _dropin.fitness(args[:27])

@@ -1,0 +1,82 @@
+"""In-tree build of the native library ``tomography_gb300/_lib/libtomography_gb300.so``.
+
+Each translation unit is compiled by nvcc for sm_103a only (GB300), in
+parallel, then linked into one shared library that exports the C ABI of
+``include/tomography.h`` and the C++ drop-in of ``include/tomography_fdtd.hpp``.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+OUT_DIR = os.path.join(HERE, "_lib")
+OBJ_DIR = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT_DIR, "libtomography_gb300.so")
+REPO = os.path.dirname(HERE)
+
+SOURCES = [
+    "advance_f32.cu",
+    "advance_f64.cu",
+    "engine.cu",
+    "serve.cu",
+    "capi.cpp",
+    "fdtd_gpu_dropin.cpp",
+]
+HEADERS = ["solve_desc.h", "fdtd_advance.cuh", "aux_kernels.cuh", "engine.h", "engine_impl.cuh"]
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+              "--expt-relaxed-constexpr", "-I", os.path.join(REPO, "include")]
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _deps() -> list[str]:
+    out = [os.path.join(CSRC, h) for h in HEADERS if os.path.exists(os.path.join(CSRC, h))]
+    out.append(os.path.join(REPO, "include", "tomography.h"))
+    out.append(__file__)
+    return out
+
+
+def _compile(src: str, extra: list[str]) -> str:
+    obj = os.path.join(OBJ_DIR, os.path.basename(src) + ".o")
+    srcp = os.path.join(CSRC, src)
+    newest = max([os.path.getmtime(srcp)] + [os.path.getmtime(d) for d in _deps()])
+    if os.path.exists(obj) and os.path.getmtime(obj) >= newest:
+        return obj
+    cmd = [nvcc()] + ARCH + NVCC_FLAGS + extra + ["-c", srcp, "-o", obj]
+    proc = subprocess.run(cmd, capture_output=True, text=True)
+    if proc.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {src}:\n{proc.stdout}\n{proc.stderr}")
+    return obj
+
+
+def build(verbose: bool = False, extra: list[str] | None = None) -> str:
+    os.makedirs(OUT_DIR, exist_ok=True)
+    os.makedirs(OBJ_DIR, exist_ok=True)
+    extra = extra or []
+    srcs = [s for s in SOURCES if os.path.exists(os.path.join(CSRC, s))]
+    with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(lambda s: _compile(s, extra), srcs))
+    if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+        proc = subprocess.run(cmd, capture_output=True, text=True)
+        if proc.returncode != 0:
+            raise RuntimeError(f"link failed:\n{proc.stdout}\n{proc.stderr}")
+    if verbose:
+        print(LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    build(verbose=True, extra=sys.argv[1:])

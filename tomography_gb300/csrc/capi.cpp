@@ -1,0 +1,116 @@
+// C ABI entry points (include/tomography.h) over the engine.
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/tomography.h"
+#include "engine.h"
+
+struct tomo_handle {
+    tomo::EngineBase* eng = nullptr;
+    tomo_spec spec{};
+};
+
+using tomo::fail;
+
+extern "C" {
+
+int tomo_spec_reference(tomo_spec* spec, int cpu_variant) { return tomo::spec_reference(spec, cpu_variant); }
+int tomo_spec_breast(tomo_spec* spec, int config) { return tomo::spec_breast(spec, config); }
+int tomo_num_params(const tomo_spec* spec) { return tomo::num_params(spec); }
+int tomo_num_excitations(const tomo_spec* spec) { return tomo::num_excitations(spec); }
+
+int tomo_create(const tomo_spec* spec, tomo_handle** out) {
+    if (!spec || !out) return fail(TOMO_EINVAL, "tomo_create: NULL argument");
+    *out = nullptr;
+    tomo::EngineBase* e = nullptr;
+    int rc = tomo::create_engine(spec, &e);
+    if (rc) return rc;
+    tomo_handle* h = new tomo_handle;
+    h->eng = e;
+    h->spec = *spec;
+    *out = h;
+    return TOMO_OK;
+}
+
+void tomo_destroy(tomo_handle* h) {
+    if (!h) return;
+    delete h->eng;
+    delete h;
+}
+
+int tomo_set_stream(tomo_handle* h, void* stream) {
+    if (!h) return fail(TOMO_EINVAL, "NULL handle");
+    return h->eng->set_stream(stream);
+}
+
+int tomo_set_memory_budget(tomo_handle* h, uint64_t bytes) {
+    if (!h) return fail(TOMO_EINVAL, "NULL handle");
+    return h->eng->set_budget(bytes);
+}
+
+int tomo_set_target(tomo_handle* h, const float* target, size_t n) {
+    if (!h) return fail(TOMO_EINVAL, "NULL handle");
+    return h->eng->set_target(target, n);
+}
+
+int tomo_fitness(tomo_handle* h, const double* args, size_t n_args, double* fitness) {
+    if (!h || !args || !fitness) return fail(TOMO_EINVAL, "tomo_fitness: NULL argument");
+    tomo_outputs o{};
+    o.fitness = fitness;
+    return h->eng->forward(args, 1, n_args, &o);
+}
+
+int tomo_fitness_batch(tomo_handle* h, const double* args, size_t n_cand, size_t n_param, double* fitness) {
+    if (!h || !args || !fitness) return fail(TOMO_EINVAL, "tomo_fitness_batch: NULL argument");
+    tomo_outputs o{};
+    o.fitness = fitness;
+    return h->eng->forward(args, n_cand, n_param, &o);
+}
+
+int tomo_forward(tomo_handle* h, const double* args, size_t n_cand, size_t n_param, const tomo_outputs* out) {
+    if (!h || !args) return fail(TOMO_EINVAL, "tomo_forward: NULL argument");
+    tomo_outputs none{};
+    return h->eng->forward(args, n_cand, n_param, out ? out : &none);
+}
+
+int tomo_submit(tomo_handle* h, const double* args, size_t n_cand, size_t n_param, uint64_t* ticket) {
+    if (!h || !args || !ticket) return fail(TOMO_EINVAL, "tomo_submit: NULL argument");
+    return h->eng->submit(args, n_cand, n_param, ticket);
+}
+
+int tomo_submit_spec(tomo_handle* h, const tomo_spec* spec, const double* args, size_t n_cand, size_t n_param,
+                     uint64_t* ticket) {
+    if (!h || !args || !ticket) return fail(TOMO_EINVAL, "tomo_submit_spec: NULL argument");
+    return h->eng->submit_spec(spec, args, n_cand, n_param, ticket);
+}
+
+int tomo_set_target_spec(tomo_handle* h, const tomo_spec* spec, const float* target, size_t n) {
+    if (!h) return fail(TOMO_EINVAL, "NULL handle");
+    return h->eng->set_target_spec(spec, target, n);
+}
+
+int tomo_serve_step(tomo_handle* h, int* n_active) {
+    if (!h) return fail(TOMO_EINVAL, "NULL handle");
+    return h->eng->serve_step(n_active);
+}
+
+int tomo_poll(tomo_handle* h, uint64_t ticket, double* fitness) {
+    if (!h) return fail(TOMO_EINVAL, "NULL handle");
+    return h->eng->poll(ticket, fitness);
+}
+
+int tomo_cancel(tomo_handle* h, uint64_t ticket) {
+    if (!h) return fail(TOMO_EINVAL, "NULL handle");
+    return h->eng->cancel(ticket);
+}
+
+int tomo_get_stats(tomo_handle* h, tomo_stats* stats) {
+    if (!h) return fail(TOMO_EINVAL, "NULL handle");
+    return h->eng->stats(stats);
+}
+
+const char* tomo_last_error(void) { return tomo::g_last_error.c_str(); }
+const char* tomo_version(void) { return "tomography_gb300 0.1"; }
+
+}  // extern "C"

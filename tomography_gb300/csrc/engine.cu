@@ -1,0 +1,674 @@
+// Host engine of the forward FDTD fitness path and its C ABI (include/tomography.h).
+//
+// Lifecycle of one batch (tomo_fitness_batch / tomo_forward):
+//   host: unpack candidate arguments into per-material (eps_inf, del_eps, sigma)
+//         triples and ellipse geometry (FDTD_GPU.cu:657-693 / FDTD_CPU.cxx:682-698)
+//   H2D : one packed upload
+//   GPU : material maps + FP64 coefficient tables, zero state, a CUDA graph of
+//         ceil(steps/T) advance launches (each followed by a progress bump),
+//         far field, misfit
+//   D2H : fitness (plus optional traces / far field)
+// Device buffers persist across calls (the reference allocates and frees ~30
+// buffers inside every call, FDTD_GPU.cu:858-1106).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "engine_impl.cuh"
+
+namespace tomo {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+const double kC0 = 1.0 / std::sqrt(kMu0D * kEps0D);
+const double kEta0 = std::sqrt(kMu0D / kEps0D);
+
+// ---------------------------------------------------------------------------
+// Presets
+static void spec_zero(tomo_spec* s) { std::memset(s, 0, sizeof(*s)); }
+
+int spec_reference(tomo_spec* s, int cpu_variant) {
+    if (!s) return fail(TOMO_EINVAL, "spec is NULL");
+    spec_zero(s);
+    // FDTD_common.hxx:3-59
+    const double br = 0.0315, dx = 0.001;
+    s->mode = cpu_variant ? TOMO_MODE_REFERENCE_CPU : TOMO_MODE_REFERENCE_GPU;
+    s->precision = TOMO_FP32;
+    s->nx = s->ny = (int)std::ceil(12.7 * br / dx);
+    s->dx = dx;
+    s->dt = dx / kC0 / 2;
+    s->steps = 2000;
+    s->ncpml = 10;
+    s->cpml_grading = 2;
+    s->cpml_sigma_max = (2 + 1) / (150 * kPiD * dx);
+    s->cpml_kappa_max = 10;
+    s->cpml_alpha_max = 0.01;
+    s->cpml_alpha_min = 0.0;
+    s->tau = 7e-12;
+    s->breast_radius = br;
+    s->npatch = cpu_variant ? 9 : 3;
+    s->n_excitations = 4;
+    s->pw_tau = 3.3445267e-11;
+    s->pw_t0 = std::sqrt(20.0) * s->pw_tau;
+    s->pw_l = -br;
+    s->pw_centred = cpu_variant ? 0 : 1;
+    s->nan_clamp = cpu_variant ? 0 : 1;
+    s->nf2ff_d = (int)std::floor(3.2 * br / dx);
+    s->nfreq = 10;
+    for (int f = 0; f < 10; ++f) s->freqs[f] = 1e9 + (1e10 - 1e9) / 9 * f;
+    s->n_angles = 100;
+    s->ff_norm = 1;
+    s->misfit = cpu_variant ? 1 : 0;
+    return TOMO_OK;
+}
+
+int spec_breast(tomo_spec* s, int config) {
+    if (!s) return fail(TOMO_EINVAL, "spec is NULL");
+    if (config < 0 || config > 4) return fail(TOMO_EINVAL, "breast config must be 0..4");
+    spec_zero(s);
+    s->mode = TOMO_MODE_BREAST;
+    s->precision = TOMO_FP32;
+    s->dx = 0.5e-3;
+    s->nx = s->ny = 200;
+    s->steps = 1000;
+    s->ncpml = 10;
+    s->n_ellipses = 3;
+    s->n_antennas = 16;
+    s->n_tx = 1;
+    s->antenna_radius = 45e-3;
+    s->nfreq = 3;
+    s->freqs[0] = 3e9; s->freqs[1] = 6e9; s->freqs[2] = 9e9;
+    s->n_angles = 72;
+    s->disc_radius = 35e-3;
+    s->disc_eps_inf = 3.1; s->disc_del_eps = 1.6; s->disc_sigma = 0.036;
+    switch (config) {
+        case 0: break;
+        case 1:
+            s->nx = s->ny = 400; s->ncpml = 12; s->steps = 3000; s->n_ellipses = 8; s->n_tx = 16;
+            break;
+        case 2:
+            s->nx = s->ny = 600; s->dx = 0.25e-3; s->ncpml = 12; s->steps = 6000;
+            s->n_antennas = 32; s->n_tx = 32; s->antenna_radius = 70e-3;
+            s->nfreq = 8;
+            for (int f = 0; f < 8; ++f) s->freqs[f] = 2e9 + 1e9 * f;
+            s->n_angles = 360;
+            break;
+        case 3:
+            // serving default request: 256^2, breast (35 mm disc) at 70% of the domain
+            s->nx = s->ny = 256; s->dx = 0.1 / 256; s->ncpml = 10; s->steps = 4 * 256;
+            s->n_ellipses = 8; s->n_tx = 16; s->antenna_radius = 42e-3;
+            break;
+        case 4:
+            s->nx = s->ny = 2048; s->dx = 0.125e-3; s->ncpml = 16; s->steps = 20000;
+            s->n_antennas = 32; s->n_tx = 32; s->n_ellipses = 16; s->antenna_radius = 70e-3;
+            s->disc_eps_inf = 15.9; s->disc_del_eps = 23.8; s->disc_sigma = 0.83;   // skin layer
+            s->nfreq = 16;
+            for (int f = 0; f < 16; ++f) s->freqs[f] = 1e9 + 0.5e9 * f;
+            s->n_angles = 720;
+            break;
+    }
+    s->dt = 0.99 * s->dx / (kC0 * std::sqrt(2.0));
+    s->cpml_grading = 3;
+    s->cpml_sigma_max = 0.8 * (3 + 1) / (kEta0 * s->dx);
+    s->cpml_kappa_max = 5;
+    s->cpml_alpha_max = 0.05;
+    s->cpml_alpha_min = 0;
+    s->tau = 13e-12;
+    s->bg_eps_inf = 9; s->bg_del_eps = 0; s->bg_sigma = 0;
+    s->src_f0 = 6e9;
+    const double fmax = kC0 / (20 * s->dx * std::sqrt(s->bg_eps_inf));
+    const double band = std::max(fmax - s->src_f0, 1e9);
+    s->src_tau = std::sqrt(std::log(10.0)) / (kPiD * band);
+    s->src_t0 = 4 * s->src_tau;
+    s->src_amp = 0;
+    s->nf2ff_d = s->ncpml + 3;
+    s->ff_norm = 0;
+    s->misfit = 2;
+    return TOMO_OK;
+}
+
+int num_params(const tomo_spec* s) {
+    if (!s) return -1;
+    if (s->mode == TOMO_MODE_REFERENCE_GPU) return s->npatch * s->npatch * 3;
+    if (s->mode == TOMO_MODE_REFERENCE_CPU) return s->npatch * s->npatch * 2;
+    return 8 * s->n_ellipses;
+}
+
+int num_excitations(const tomo_spec* s) {
+    if (!s) return -1;
+    return s->mode == TOMO_MODE_BREAST ? s->n_tx : s->n_excitations;
+}
+
+
+int validate_spec(const tomo_spec* s) {
+    if (!s) return fail(TOMO_EINVAL, "spec is NULL");
+    if (s->mode < 0 || s->mode > 2) return fail(TOMO_EINVAL, "unknown mode");
+    if (s->precision != TOMO_FP32 && s->precision != TOMO_FP64) return fail(TOMO_EINVAL, "unknown precision");
+    if (s->nx < 16 || s->ny < 16 || s->nx > 8190 || s->ny > 8190) return fail(TOMO_EINVAL, "grid size out of range");
+    if (s->steps < 1) return fail(TOMO_EINVAL, "steps must be positive");
+    if (!(s->dx > 0) || !(s->dt > 0)) return fail(TOMO_EINVAL, "dx and dt must be positive");
+    if (s->ncpml < 0 || s->ncpml > 64 || 2 * s->ncpml + 4 > std::min(s->nx, s->ny))
+        return fail(TOMO_EINVAL, "ncpml out of range");
+    if (s->nfreq < 0 || s->nfreq > TOMO_MAX_FREQS) return fail(TOMO_EINVAL, "nfreq out of range");
+    if (s->nfreq > 0 && (s->nf2ff_d < 1 || 2 * s->nf2ff_d + 4 > std::min(s->nx, s->ny)))
+        return fail(TOMO_EINVAL, "nf2ff_d out of range");
+    if (s->nfreq > 0 && s->n_angles < 0) return fail(TOMO_EINVAL, "n_angles out of range");
+    if (s->mode != TOMO_MODE_BREAST) {
+        if (s->nx != s->ny) return fail(TOMO_EINVAL, "reference modes need a square grid");
+        if (s->npatch < 1 || s->npatch * s->npatch + 1 > kMaxMat) return fail(TOMO_EINVAL, "npatch out of range");
+        if (s->n_excitations < 1) return fail(TOMO_EINVAL, "n_excitations must be positive");
+        if (!(s->pw_tau > 0)) return fail(TOMO_EINVAL, "pw_tau must be positive");
+    } else {
+        if (s->n_ellipses < 0 || s->n_ellipses + 2 > kMaxMat) return fail(TOMO_EINVAL, "n_ellipses out of range");
+        if (s->n_antennas < 1 || s->n_antennas > kMaxRx) return fail(TOMO_EINVAL, "n_antennas out of range");
+        if (s->n_tx < 1 || s->n_tx > s->n_antennas) return fail(TOMO_EINVAL, "n_tx out of range");
+        if (!(s->src_tau > 0)) return fail(TOMO_EINVAL, "src_tau must be positive");
+    }
+    if (!(s->tau > 0)) return fail(TOMO_EINVAL, "tau must be positive");
+    return TOMO_OK;
+}
+
+bool same_problem(const tomo_spec& a, const tomo_spec& b) {
+    tomo_spec x = a, y = b;
+    x.steps_per_launch = y.steps_per_launch = 0;
+    x.cols_per_lane = y.cols_per_lane = 0;
+    return std::memcmp(&x, &y, sizeof(tomo_spec)) == 0;
+}
+
+static void cpml_profile(const tomo_spec& s, std::vector<double>& out) {
+    // FDTD_GPU.cu:748-806; kappa stored as its reciprocal for the device.
+    const int nc = s.ncpml;
+    out.assign(6 * (size_t)nc, 0.0);
+    for (int i = 0; i < nc; ++i) {
+        double rho = (i + 0.25) / nc;
+        double se = s.cpml_sigma_max * std::pow(rho, s.cpml_grading);
+        double ke = std::pow(rho, s.cpml_grading) * (s.cpml_kappa_max - 1) + 1;
+        double ale = s.cpml_alpha_min + (s.cpml_alpha_max - s.cpml_alpha_min) * rho;
+        double be = std::exp(-(s.dt / kEps0D) * (se / ke + ale));
+        double ae = ((be - 1) * se) / (s.dx * (se * ke + ale * ke * ke));
+        rho = (i + 0.75) / nc;
+        double sm = (kMu0D / kEps0D) * s.cpml_sigma_max * std::pow(rho, s.cpml_grading);
+        double km = std::pow(rho, s.cpml_grading) * (s.cpml_kappa_max - 1) + 1;
+        double alm = (kMu0D / kEps0D) * (s.cpml_alpha_min + (s.cpml_alpha_max - s.cpml_alpha_min) * rho);
+        double bm = std::exp(-(s.dt / kMu0D) * (sm / km + alm));
+        double am = (bm - 1) * sm / (s.dx * (sm * km + alm * km * km));
+        out[0 * nc + i] = 1.0 / ke;
+        out[1 * nc + i] = be;
+        out[2 * nc + i] = ae;
+        out[3 * nc + i] = 1.0 / km;
+        out[4 * nc + i] = bm;
+        out[5 * nc + i] = am;
+    }
+}
+
+static void contour_point(int nx, int ny, int d, int index, int* x, int* y, int* face) {
+    // FDTD_common.cxx:4-46
+    int l1 = nx - 2 * d - 2, l2 = l1 + (ny - 2 * d), l3 = l2 + l1;
+    if (index < l1) { *x = index + d + 1; *y = d; *face = 0; }
+    else if (index < l2) { *x = nx - d - 1; *y = index - l1 + d; *face = 1; }
+    else if (index < l3) { *x = nx - d - 2 - (index - l2); *y = ny - d - 1; *face = 2; }
+    else { *x = d; *y = ny - d - 1 - (index - l3); *face = 3; }
+}
+
+int build_class(const tomo_spec& s, ProblemClass& pc) {
+    TOMO_TRY(validate_spec(&s));
+    pc.spec = s;
+    pc.nx = s.nx; pc.ny = s.ny; pc.nc = s.ncpml; pc.S = s.steps;
+    pc.nfreq = s.nfreq;
+    pc.nang = s.nfreq > 0 ? s.n_angles : 0;
+    pc.C = s.nfreq > 0 ? 2 * s.nx + 2 * s.ny - 8 * s.nf2ff_d - 4 : 0;
+    pc.n_exc = num_excitations(&s);
+    pc.nparam = num_params(&s);
+    pc.dt = s.dt;
+    pc.chez = (s.dt / s.dx) / kMu0D;
+    pc.Kp = (1 - s.dt / (2 * s.tau)) / (1 + s.dt / (2 * s.tau));
+    pc.pitch = ((kPadLeft + s.nx + 1 + kPadRight) + 31) / 32 * 32;
+    pc.mpitch = (kMatPadLeft + s.nx + 1 + 160 + 31) / 32 * 32;
+    cpml_profile(s, pc.cpml);
+    // running-DFT phasors (FDTD_GPU.cu:251-276): J at n dt, M at (n + 1/2) dt, times dt
+    pc.phasor.assign((size_t)pc.S * std::max(pc.nfreq, 1) * 4, 0.0);
+    for (int n = 0; n < pc.S; ++n)
+        for (int f = 0; f < pc.nfreq; ++f) {
+            double w = 2 * kPiD * s.freqs[f];
+            double* p = &pc.phasor[((size_t)n * pc.nfreq + f) * 4];
+            p[0] = s.dt * std::cos(w * n * s.dt);
+            p[1] = -s.dt * std::sin(w * n * s.dt);
+            p[2] = s.dt * std::cos(w * (n + 0.5) * s.dt);
+            p[3] = -s.dt * std::sin(w * (n + 0.5) * s.dt);
+        }
+    pc.rx.clear();
+    pc.patchmap.clear();
+    if (s.mode == TOMO_MODE_BREAST) {
+        pc.nmat = 2 + s.n_ellipses;
+        pc.nrx = s.n_antennas;
+        pc.rx.resize(2 * (size_t)pc.nrx);
+        for (int a = 0; a < pc.nrx; ++a) {
+            double th = 2 * kPiD * a / pc.nrx;
+            pc.rx[2 * a] = (int)std::lround(s.nx / 2.0 + (s.antenna_radius / s.dx) * std::cos(th));
+            pc.rx[2 * a + 1] = (int)std::lround(s.ny / 2.0 + (s.antenna_radius / s.dx) * std::sin(th));
+            if (pc.rx[2 * a] < 1 || pc.rx[2 * a] > s.nx - 1 || pc.rx[2 * a + 1] < 1 || pc.rx[2 * a + 1] > s.ny - 1)
+                return fail(TOMO_EINVAL, "antenna outside the grid");
+        }
+        // zero-mean Gaussian-modulated sine current source centred at src_f0
+        pc.src_amp = s.src_amp > 0 ? s.src_amp : (2 * s.bg_eps_inf * kEps0D + s.bg_sigma * s.dt) / (2 * s.dt);
+        pc.wave.resize(pc.S);
+        for (int n = 0; n < pc.S; ++n) {
+            double t = (n + 0.5) * s.dt - s.src_t0;
+            pc.wave[n] = pc.src_amp * std::sin(2 * kPiD * s.src_f0 * t) * std::exp(-(t / s.src_tau) * (t / s.src_tau));
+        }
+    } else {
+        pc.nmat = 1 + s.npatch * s.npatch;
+        pc.nrx = 0;
+        pc.src_amp = 0;
+        pc.wave.assign(1, 0.0);
+        // fixed patch map (FDTD_GPU.cu:718-731, 544-551; FDTD_CPU.cxx:530-537, 1078-1164)
+        pc.patchmap.assign((size_t)(s.ny + 1) * pc.mpitch, 0);
+        const double br = s.breast_radius, dx = s.dx, cell = 2 * br / (s.npatch * dx);
+        for (int j = 0; j <= s.ny; ++j)
+            for (int i = 0; i <= s.nx; ++i) {
+                double rx = ((float)i - s.nx / 2) * dx, ry = ((float)j - s.ny / 2) * dx;
+                float radius = (float)std::sqrt(rx * rx + ry * ry);
+                uint8_t m = 0;
+                if (radius <= br) {
+                    int xc = (int)((double)(i - (s.nx / 2 - (int)(br / dx))) / cell);
+                    int yc = (int)((j - (s.ny / 2 - br / dx)) / cell);
+                    m = (uint8_t)(1 + xc + s.npatch * yc);
+                }
+                pc.patchmap[(size_t)j * pc.mpitch + kMatPadLeft + i] = m;
+            }
+    }
+    // far-field geometry (FDTD_GPU.cu:579-625): contour point relative to the
+    // transform origin (nx/2 - 1, ny/2 - 1) with nx/2 in float division, metres
+    pc.ffgeom.resize(3 * (size_t)pc.C);
+    for (int c = 0; c < pc.C; ++c) {
+        int x, y, face;
+        contour_point(s.nx, s.ny, s.nf2ff_d, c, &x, &y, &face);
+        double flx = x, fly = y;
+        if (face == 0 || face == 2) fly += 0.5; else flx += 0.5;
+        pc.ffgeom[3 * c + 0] = s.dx * (flx - (s.nx / 2.0 - 1));
+        pc.ffgeom[3 * c + 1] = s.dx * (fly - (s.ny / 2.0 - 1));
+        pc.ffgeom[3 * c + 2] = face;
+    }
+    pc.ffang.resize(2 * (size_t)pc.nang);
+    for (int a = 0; a < pc.nang; ++a) {
+        double phi = 2 * kPiD / pc.nang * a;
+        pc.ffang[2 * a] = std::cos(phi);
+        pc.ffang[2 * a + 1] = std::sin(phi);
+    }
+    return TOMO_OK;
+}
+
+SolveLayout solve_layout(const ProblemClass& pc, size_t real_bytes) {
+    SolveLayout L;
+    const size_t rows = (size_t)pc.ny + 1;
+    L.field_elems = rows * pc.pitch;
+    L.psi_elems = (size_t)4 * pc.nc * (pc.ny + 1) + (size_t)4 * pc.nc * (pc.nx + 1) + 32;
+    L.psi_elems = (L.psi_elems + 31) / 32 * 32;
+    L.tr_stride = std::max<size_t>((size_t)pc.nrx * pc.S, 1);
+    L.tr_stride = (L.tr_stride + 31) / 32 * 32;
+    L.acc_stride = std::max<size_t>((size_t)pc.nfreq * pc.C * 8, 8);
+    const int tmax = 8;
+    L.per_solve = 8 * L.field_elems + (size_t)(tmax + 1) * L.psi_elems + L.tr_stride + L.acc_stride;
+    L.per_solve = (L.per_solve + 63) / 64 * 64;
+    L.mat_stride = rows * pc.mpitch;
+    (void)real_bytes;
+    return L;
+}
+
+int unpack_args(const ProblemClass& pc, const double* args, size_t ncand, size_t nparam, Unpacked& u) {
+    // upload layout: [ncand][kMaxMat][3] material triples, then [ncand][K][6] ellipses
+    const tomo_spec& s = pc.spec;
+    if (!args || ncand == 0) return fail(TOMO_EINVAL, "no candidates");
+    if ((int)nparam != pc.nparam)
+        return fail(TOMO_EINVAL, "expected " + std::to_string(pc.nparam) + " parameters per candidate, got " +
+                                     std::to_string(nparam));
+    const int K = s.mode == TOMO_MODE_BREAST ? s.n_ellipses : 0;
+    u.ncand = ncand;
+    u.upload.assign(ncand * kMaxMat * 3 + ncand * (size_t)K * 6, 0.0);
+    u.bbox.assign(ncand * 4, 0);
+    for (size_t c = 0; c < ncand; ++c) {
+        const double* a = args + c * nparam;
+        double* mp = &u.upload[c * kMaxMat * 3];
+        for (size_t i = 0; i < nparam; ++i)
+            if (!std::isfinite(a[i])) return fail(TOMO_EINVAL, "non-finite candidate parameter");
+        int* bb = &u.bbox[c * 4];
+        if (s.mode != TOMO_MODE_BREAST) {
+            // FDTD_GPU.cu:657-693, 718-738 (3x3: eps_inf, del_eps, sigma) and
+            // FDTD_CPU.cxx:682-698, 1078-1164 (9x9: eps_r, sigma); the reference
+            // stores the arguments as float.
+            const int np2 = s.npatch * s.npatch;
+            mp[0] = 1; mp[1] = 0; mp[2] = 0;
+            for (int p = 0; p < np2; ++p) {
+                if (s.mode == TOMO_MODE_REFERENCE_GPU) {
+                    mp[3 * (1 + p) + 0] = (double)(float)a[p];
+                    mp[3 * (1 + p) + 1] = (double)(float)a[np2 + p];
+                    mp[3 * (1 + p) + 2] = (double)(float)a[2 * np2 + p];
+                } else {
+                    mp[3 * (1 + p) + 0] = (double)(float)a[p];
+                    mp[3 * (1 + p) + 1] = 0;
+                    mp[3 * (1 + p) + 2] = (double)(float)a[np2 + p];
+                }
+                if (!(mp[3 * (1 + p)] > 0)) return fail(TOMO_EINVAL, "permittivity must be positive");
+            }
+            const int r = (int)std::ceil(s.breast_radius / s.dx) + 2;
+            bb[0] = std::max(1, s.nx / 2 - r); bb[1] = std::min(s.nx - 1, s.nx / 2 + r);
+            bb[2] = std::max(1, s.ny / 2 - r); bb[3] = std::min(s.ny - 1, s.ny / 2 + r);
+            continue;
+        }
+        mp[0] = s.bg_eps_inf; mp[1] = s.bg_del_eps; mp[2] = s.bg_sigma;
+        mp[3] = s.disc_eps_inf; mp[4] = s.disc_del_eps; mp[5] = s.disc_sigma;
+        double* el = &u.upload[ncand * kMaxMat * 3 + c * (size_t)K * 6];
+        double xlo = 1e30, xhi = -1e30, ylo = 1e30, yhi = -1e30;
+        auto grow = [&](double cx, double cy, double r) {
+            xlo = std::min(xlo, cx - r); xhi = std::max(xhi, cx + r);
+            ylo = std::min(ylo, cy - r); yhi = std::max(yhi, cy + r);
+        };
+        bool everywhere = s.bg_del_eps != 0;
+        if (s.disc_radius > 0 && s.disc_del_eps != 0) grow(0, 0, s.disc_radius);
+        for (int k = 0; k < K; ++k) {
+            const double* e = a + 8 * k;
+            if (!(e[2] > 0) || !(e[3] > 0)) return fail(TOMO_EINVAL, "ellipse semi-axes must be positive");
+            if (!(e[5] > 0) || e[6] < 0 || e[7] < 0) return fail(TOMO_EINVAL, "ellipse material out of range");
+            el[6 * k + 0] = e[0];
+            el[6 * k + 1] = e[1];
+            el[6 * k + 2] = e[2];
+            el[6 * k + 3] = e[3];
+            el[6 * k + 4] = std::cos(e[4]);
+            el[6 * k + 5] = std::sin(e[4]);
+            mp[3 * (2 + k) + 0] = e[5];
+            mp[3 * (2 + k) + 1] = e[6];
+            mp[3 * (2 + k) + 2] = e[7];
+            if (e[6] != 0) grow(e[0], e[1], std::max(e[2], e[3]));
+        }
+        // Jp can be non-zero only where del_eps != 0: conservative cell box
+        auto cell = [&](double v, int n, bool up) {
+            double c = v / s.dx + 0.5 * n;
+            double r = up ? std::ceil(c) + 1 : std::floor(c) - 1;
+            r = std::max(1.0, std::min((double)(n - 1), r));
+            return (int)r;
+        };
+        if (everywhere) { bb[0] = 1; bb[1] = s.nx - 1; bb[2] = 1; bb[3] = s.ny - 1; }
+        else if (xhi < xlo) { bb[0] = 1; bb[1] = 0; bb[2] = 1; bb[3] = 0; }
+        else {
+            bb[0] = cell(xlo, s.nx, false); bb[1] = cell(xhi, s.nx, true);
+            bb[2] = cell(ylo, s.ny, false); bb[3] = cell(yhi, s.ny, true);
+        }
+    }
+    return TOMO_OK;
+}
+
+// ------------------------------------------------------------------- EngineT
+template <typename Real>
+EngineT<Real>::~EngineT() {
+    serve_release();
+    if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+    if (own_stream_ && stream_) cudaStreamDestroy(stream_);
+    for (auto& e : ev_)
+        if (e) cudaEventDestroy(e);
+}
+
+template <typename Real>
+int EngineT<Real>::init(const ProblemClass& pc) {
+    CUDA_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    own_stream_ = true;
+    for (auto& e : ev_) CUDA_TRY(cudaEventCreate(&e));
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    CUDA_TRY(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, dev));
+    TOMO_TRY(cd_.init(pc));
+    // tuning: explicit spec values, else environment, else defaults
+    T_ = pc.spec.steps_per_launch;
+    cols_ = pc.spec.cols_per_lane;
+    if (T_ <= 0) {
+        const char* e = std::getenv("TOMO_T");
+        T_ = e ? std::atoi(e) : (sizeof(Real) == 4 ? 4 : 1);
+    }
+    if (cols_ <= 0) {
+        const char* e = std::getenv("TOMO_COLS");
+        cols_ = e ? std::atoi(e) : 1;
+    }
+    if (!advance_kernel_for<Real>(T_, cols_, advance_mode(pc.spec)))
+        return fail(TOMO_EINVAL, "unsupported (steps_per_launch, cols_per_lane) pair for this mode and precision");
+    return TOMO_OK;
+}
+
+template <typename Real>
+int EngineT<Real>::set_stream(void* s) {
+    CUDA_TRY(cudaStreamSynchronize(stream_));
+    if (own_stream_) {
+        cudaStreamDestroy(stream_);
+        own_stream_ = false;
+    }
+    if (s) {
+        stream_ = (cudaStream_t)s;
+    } else {
+        CUDA_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+        own_stream_ = true;
+    }
+    invalidate_graph();
+    return TOMO_OK;
+}
+
+template <typename Real>
+int EngineT<Real>::set_budget(uint64_t b) {
+    budget_ = b ? b : (uint64_t)150 << 30;
+    return TOMO_OK;
+}
+
+template <typename Real>
+int EngineT<Real>::ensure_batch(int ncand) {
+    const ProblemClass& pc = cd_.pc;
+    const SolveLayout& L = cd_.lay;
+    const int nsolves = ncand * pc.n_exc;
+    const size_t need = (size_t)nsolves * L.per_solve * sizeof(Real);
+    if (need > budget_)
+        return fail(TOMO_ENOMEM_BUDGET, "batch needs " + std::to_string(need >> 20) + " MiB, budget " +
+                                            std::to_string(budget_ >> 20) + " MiB");
+    if (ncand > cap_cand_) {
+        invalidate_graph();
+        cap_cand_ = 0;
+        TOMO_TRY(d_state_.ensure(need));
+        if (pc.spec.mode == TOMO_MODE_BREAST) TOMO_TRY(d_mats_.ensure(L.mat_stride * ncand));
+        TOMO_TRY(d_tabs_.ensure(sizeof(Real) * kMaxMat * kMatCoef * ncand));
+        TOMO_TRY(d_descs_.ensure(sizeof(SolveDesc<Real>) * nsolves));
+        TOMO_TRY(d_partials_.ensure(sizeof(double) * 2 * nsolves));
+        TOMO_TRY(d_fit_.ensure(sizeof(double) * ncand));
+        TOMO_TRY(d_flag_.ensure(sizeof(int) * 4));
+        if (pc.nang > 0) {
+            TOMO_TRY(d_D_.ensure(sizeof(float) * (size_t)nsolves * pc.nfreq * pc.nang));
+            TOMO_TRY(d_P_.ensure(sizeof(float) * (size_t)nsolves * pc.nfreq * pc.nang));
+        }
+        cap_cand_ = ncand;
+    }
+    std::vector<WorkItem> items;
+    append_items(items, 0, nsolves, pc.nx, T_, cols_);
+    if (nsolves != nsolves_ || (int)items.size() != nitems_ || ncand != cur_cand_) {
+        invalidate_graph();
+        TOMO_TRY(d_items_.ensure(sizeof(WorkItem) * items.size()));
+        CUDA_TRY(cudaMemcpyAsync(d_items_.p, items.data(), sizeof(WorkItem) * items.size(), cudaMemcpyHostToDevice,
+                                 stream_));
+    }
+    nsolves_ = nsolves;
+    nitems_ = (int)items.size();
+    cur_cand_ = ncand;
+    return TOMO_OK;
+}
+
+template <typename Real>
+int EngineT<Real>::build_graph(int nlaunch) {
+    if (graph_exec_ && graph_cand_ == cur_cand_ && graph_T_ == T_ && graph_cols_ == cols_ && graph_launches_ == nlaunch)
+        return TOMO_OK;
+    invalidate_graph();
+    int blocks = 0;
+    size_t smem = 0;
+    TOMO_TRY(advance_grid<Real>(T_, cols_, advance_mode(cd_.pc.spec), nitems_, num_sms_, &blocks, &smem));
+    cudaGraph_t graph;
+    CUDA_TRY(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+    for (int l = 0; l < nlaunch; ++l)
+        launch_advance<Real>(T_, cols_, advance_mode(cd_.pc.spec), blocks, smem, d_descs_.as<SolveDesc<Real>>(),
+                             d_items_.as<WorkItem>(), nitems_, nsolves_, stream_);
+    cudaError_t ce = cudaStreamEndCapture(stream_, &graph);
+    if (ce != cudaSuccess) return fail(TOMO_ECUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+    ce = cudaGraphInstantiate(&graph_exec_, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) {
+        graph_exec_ = nullptr;
+        return fail(TOMO_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce));
+    }
+    graph_cand_ = cur_cand_; graph_T_ = T_; graph_cols_ = cols_; graph_launches_ = nlaunch; graph_blocks_ = blocks;
+    return TOMO_OK;
+}
+
+template <typename Real>
+int EngineT<Real>::forward(const double* args, size_t ncand, size_t nparam, const tomo_outputs* out) {
+    const ProblemClass& pc = cd_.pc;
+    const tomo_spec& s = pc.spec;
+    const bool want_fit = out && out->fitness;
+    if (want_fit && !cd_.have_target) return fail(TOMO_ENOTARGET, "fitness needs a target (tomo_set_target)");
+    TOMO_TRY(unpack_args(pc, args, ncand, nparam, up_));
+    TOMO_TRY(ensure_batch((int)ncand));
+    const int nsolves = nsolves_;
+    int64_t kernels = 0, h2d = 0, d2h = 0;
+
+    TOMO_TRY(d_upload_.ensure(sizeof(double) * up_.upload.size()));
+    CUDA_TRY(cudaMemcpyAsync(d_upload_.p, up_.upload.data(), sizeof(double) * up_.upload.size(), cudaMemcpyHostToDevice,
+                             stream_));
+    h2d += sizeof(double) * up_.upload.size();
+    CUDA_TRY(cudaEventRecord(ev_[0], stream_));
+    TOMO_TRY(setup_materials<Real>(cd_, up_, d_upload_.as<double>(), d_mats_.as<uint8_t>(), d_tabs_.as<Real>(), stream_,
+                                   &kernels, nullptr));
+    CUDA_TRY(cudaMemsetAsync(d_state_.p, 0, (size_t)nsolves * cd_.lay.per_solve * sizeof(Real), stream_));
+    h_descs_.resize(nsolves);
+    fill_descs<Real>(cd_, up_, d_state_.as<Real>(), d_mats_.as<uint8_t>(), d_tabs_.as<Real>(), h_descs_.data());
+    CUDA_TRY(cudaMemcpyAsync(d_descs_.p, h_descs_.data(), sizeof(SolveDesc<Real>) * nsolves, cudaMemcpyHostToDevice,
+                             stream_));
+    h2d += sizeof(SolveDesc<Real>) * nsolves;
+
+    // time loop: ceil(S/T) advance launches + progress bumps, replayed as one CUDA graph
+    const int nlaunch = (pc.S + T_ - 1) / T_;
+    if (s.plain) {
+        // plain baseline path: every solve on its own, one launch per time step, no graph
+        std::vector<WorkItem> one;
+        append_items(one, 0, 1, pc.nx, T_, cols_);
+        const int per = (int)one.size();
+        int blocks = 0;
+        size_t smem = 0;
+        TOMO_TRY(advance_grid<Real>(T_, cols_, advance_mode(s), per, num_sms_, &blocks, &smem));
+        CUDA_TRY(cudaEventRecord(ev_[1], stream_));
+        for (int sv = 0; sv < nsolves; ++sv)
+            for (int l = 0; l < nlaunch; ++l)
+                launch_advance<Real>(T_, cols_, advance_mode(s), blocks, smem, d_descs_.as<SolveDesc<Real>>() + sv,
+                                     d_items_.as<WorkItem>(), per, 1, stream_);
+        CUDA_TRY(cudaEventRecord(ev_[2], stream_));
+        kernels += 2 * (int64_t)nlaunch * nsolves;
+    } else {
+        TOMO_TRY(build_graph(nlaunch));
+        CUDA_TRY(cudaEventRecord(ev_[1], stream_));
+        CUDA_TRY(cudaGraphLaunch(graph_exec_, stream_));
+        CUDA_TRY(cudaEventRecord(ev_[2], stream_));
+        kernels += 2 * (int64_t)nlaunch;
+    }
+
+    CUDA_TRY(cudaMemsetAsync(d_flag_.p, 0, sizeof(int) * 4, stream_));
+    float* d_trf = nullptr;
+    double* d_trd = nullptr;
+    const size_t ntr = (size_t)pc.nrx * pc.S * nsolves;
+    if (out && out->traces && pc.nrx > 0) {
+        TOMO_TRY(d_trf_.ensure(sizeof(float) * ntr));
+        d_trf = d_trf_.as<float>();
+    }
+    if (out && out->traces_f64 && pc.nrx > 0) {
+        TOMO_TRY(d_trd_.ensure(sizeof(double) * ntr));
+        d_trd = d_trd_.as<double>();
+    }
+    TOMO_TRY(post_range<Real>(cd_, ncand, h_descs_[0], want_fit, d_D_.as<float>(), d_P_.as<float>(),
+                              d_partials_.as<double>(), d_fit_.as<double>(), d_flag_.as<int>(), d_trf, d_trd, stream_,
+                              &kernels));
+    if (d_trf) {
+        CUDA_TRY(cudaMemcpyAsync(out->traces, d_trf, sizeof(float) * ntr, cudaMemcpyDeviceToHost, stream_));
+        d2h += sizeof(float) * ntr;
+    }
+    if (d_trd) {
+        CUDA_TRY(cudaMemcpyAsync(out->traces_f64, d_trd, sizeof(double) * ntr, cudaMemcpyDeviceToHost, stream_));
+        d2h += sizeof(double) * ntr;
+    }
+    if (out && pc.nang > 0) {
+        const size_t n = (size_t)nsolves * pc.nfreq * pc.nang;
+        if (out->D) {
+            CUDA_TRY(cudaMemcpyAsync(out->D, d_D_.p, sizeof(float) * n, cudaMemcpyDeviceToHost, stream_));
+            d2h += sizeof(float) * n;
+        }
+        if (out->P) {
+            CUDA_TRY(cudaMemcpyAsync(out->P, d_P_.p, sizeof(float) * n, cudaMemcpyDeviceToHost, stream_));
+            d2h += sizeof(float) * n;
+        }
+    }
+    CUDA_TRY(cudaEventRecord(ev_[3], stream_));
+    int flag = 0;
+    if (want_fit) {
+        CUDA_TRY(cudaMemcpyAsync(out->fitness, d_fit_.p, sizeof(double) * ncand, cudaMemcpyDeviceToHost, stream_));
+        CUDA_TRY(cudaMemcpyAsync(&flag, d_flag_.p, sizeof(int), cudaMemcpyDeviceToHost, stream_));
+        d2h += sizeof(double) * ncand + sizeof(int);
+    }
+    CUDA_TRY(cudaStreamSynchronize(stream_));
+    CUDA_TRY(cudaGetLastError());
+    float adv = 0, tot = 0;
+    CUDA_TRY(cudaEventElapsedTime(&adv, ev_[1], ev_[2]));
+    CUDA_TRY(cudaEventElapsedTime(&tot, ev_[0], ev_[3]));
+    stats_.advance_ms = adv;
+    stats_.total_ms = tot;
+    stats_.cell_updates = (double)nsolves * (double)s.nx * (double)s.ny * (double)pc.S;
+    stats_.launches = nlaunch;
+    stats_.kernels = kernels;
+    stats_.steps_per_launch = T_;
+    stats_.cols_per_lane = cols_;
+    stats_.h2d_bytes = h2d;
+    stats_.d2h_bytes = d2h;
+    if (flag && s.mode != TOMO_MODE_REFERENCE_GPU) return fail(TOMO_ENUMERIC, "non-finite field or fitness detected");
+    return TOMO_OK;
+}
+
+template class EngineT<float>;
+template class EngineT<double>;
+
+// ---------------------------------------------------------------------------
+int create_engine(const tomo_spec* spec, EngineBase** out) {
+    if (!out) return fail(TOMO_EINVAL, "out is NULL");
+    *out = nullptr;
+    ProblemClass pc;
+    TOMO_TRY(build_class(*spec, pc));
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(TOMO_ECUDA, "no CUDA device");
+    }
+    if (spec->precision == TOMO_FP64) {
+        auto* e = new EngineT<double>();
+        int rc = e->init(pc);
+        if (rc) { delete e; return rc; }
+        *out = e;
+    } else {
+        auto* e = new EngineT<float>();
+        int rc = e->init(pc);
+        if (rc) { delete e; return rc; }
+        *out = e;
+    }
+    return TOMO_OK;
+}
+
+}  // namespace tomo

@@ -1,0 +1,33 @@
+// Internal engine interface behind the C ABI.
+#pragma once
+#include <string>
+#include "../../include/tomography.h"
+
+namespace tomo {
+
+class EngineBase {
+   public:
+    virtual ~EngineBase() = default;
+    virtual int set_stream(void* s) = 0;
+    virtual int set_budget(uint64_t bytes) = 0;
+    virtual int set_target(const float* t, size_t n) = 0;
+    virtual int forward(const double* args, size_t ncand, size_t nparam, const tomo_outputs* out) = 0;
+    virtual int stats(tomo_stats* st) = 0;
+    virtual int submit(const double* args, size_t ncand, size_t nparam, uint64_t* ticket) = 0;
+    virtual int submit_spec(const tomo_spec* spec, const double* args, size_t ncand, size_t nparam, uint64_t* ticket) = 0;
+    virtual int set_target_spec(const tomo_spec* spec, const float* t, size_t n) = 0;
+    virtual int serve_step(int* n_active) = 0;
+    virtual int poll(uint64_t ticket, double* fitness) = 0;
+    virtual int cancel(uint64_t ticket) = 0;
+};
+
+int fail(int code, const std::string& msg);
+extern thread_local std::string g_last_error;
+
+int spec_reference(tomo_spec* s, int cpu_variant);
+int spec_breast(tomo_spec* s, int config);
+int num_params(const tomo_spec* s);
+int num_excitations(const tomo_spec* s);
+int create_engine(const tomo_spec* spec, EngineBase** out);
+
+}  // namespace tomo

@@ -1,0 +1,383 @@
+// Internal engine pieces shared by the batch path (engine.cu) and the
+// serving loop (serve.cu): spec-derived class data, argument unpacking,
+// per-range set-up / descriptor fill / post-process, and the advance launcher.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/tomography.h"
+#include "aux_kernels.cuh"
+#include "engine.h"
+#include "fdtd_advance.cuh"
+#include "solve_desc.h"
+
+#define CUDA_TRY(expr)                                                                                      \
+    do {                                                                                                    \
+        cudaError_t e_ = (expr);                                                                            \
+        if (e_ != cudaSuccess) return ::tomo::fail(TOMO_ECUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+#define TOMO_TRY(expr)            \
+    do {                          \
+        int rc_ = (expr);         \
+        if (rc_) return rc_;      \
+    } while (0)
+
+namespace tomo {
+
+extern const double kC0;
+extern const double kEta0;
+
+// --------------------------------------------------------------------- memory
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    int ensure(size_t n) {
+        if (n <= bytes && p) return TOMO_OK;
+        release();
+        if (n == 0) n = 16;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            cudaGetLastError();
+            return fail(e == cudaErrorMemoryAllocation ? TOMO_ENOMEM_BUDGET : TOMO_ECUDA,
+                        std::string("cudaMalloc(") + std::to_string(n) + "): " + cudaGetErrorString(e));
+        }
+        bytes = n;
+        return TOMO_OK;
+    }
+    template <typename U>
+    U* as() const { return reinterpret_cast<U*>(p); }
+};
+
+// ----------------------------------------------------------- spec-derived data
+struct ProblemClass {
+    tomo_spec spec;
+    int nx, ny, nc, S, C, nfreq, nang, n_exc, nrx, nparam, nmat;
+    int pitch, mpitch;
+    double dt, chez, Kp, src_amp;
+    std::vector<double> cpml;      // [6][nc]: 1/ke, be, ae, 1/km, bm, am
+    std::vector<double> phasor;    // [S][nfreq][4]
+    std::vector<double> wave;      // [S]
+    std::vector<int> rx;           // [nrx][2]
+    std::vector<uint8_t> patchmap; // reference modes, (ny+1) x mpitch
+    std::vector<double> ffgeom;    // [C][3]: X, Y, face
+    std::vector<double> ffang;     // [nang][2]: cos, sin
+};
+
+int validate_spec(const tomo_spec* s);
+int build_class(const tomo_spec& s, ProblemClass& pc);
+bool same_problem(const tomo_spec& a, const tomo_spec& b);
+
+// Per-solve memory layout (elements of Real), identical for every solve of a class.
+struct SolveLayout {
+    size_t field_elems, psi_elems, tr_stride, acc_stride, per_solve, mat_stride;
+};
+SolveLayout solve_layout(const ProblemClass& pc, size_t real_bytes);
+
+// Host-side unpacked arguments of a range of candidates.
+struct Unpacked {
+    std::vector<double> upload;   // [ncand][kMaxMat][3] then [ncand][K][6]
+    std::vector<int> bbox;        // [ncand][4] dispersive box (x0, x1, y0, y1)
+    size_t ncand = 0;
+};
+int unpack_args(const ProblemClass& pc, const double* args, size_t ncand, size_t nparam, Unpacked& u);
+
+template <typename Real>
+using AdvanceFn = void (*)(const SolveDesc<Real>*, const WorkItem*, int);
+template <typename Real>
+AdvanceFn<Real> advance_kernel_for(int T, int cols, int mode);
+
+inline int advance_mode(const tomo_spec& s) { return s.mode == TOMO_MODE_BREAST ? kModeBreast : kModeRef; }
+template <typename Real>
+size_t advance_smem_bytes(int T, int cols);
+
+// Device copy of a ProblemClass.
+template <typename Real>
+struct ClassData {
+    ProblemClass pc;
+    SolveLayout lay{};
+    DevBuf cpml, phasor, wave, rx, patch, freqs, ffgeom, ffang, target;
+    bool have_target = false;
+
+    int init(const ProblemClass& p) {
+        pc = p;
+        lay = solve_layout(pc, sizeof(Real));
+        std::vector<Real> t(pc.cpml.begin(), pc.cpml.end());
+        TOMO_TRY(cpml.ensure(sizeof(Real) * std::max<size_t>(t.size(), 1)));
+        if (!t.empty()) CUDA_TRY(cudaMemcpy(cpml.p, t.data(), sizeof(Real) * t.size(), cudaMemcpyHostToDevice));
+        std::vector<Real> ph(pc.phasor.begin(), pc.phasor.end());
+        TOMO_TRY(phasor.ensure(sizeof(Real) * std::max<size_t>(ph.size(), 4)));
+        if (!ph.empty()) CUDA_TRY(cudaMemcpy(phasor.p, ph.data(), sizeof(Real) * ph.size(), cudaMemcpyHostToDevice));
+        std::vector<Real> wv(pc.wave.begin(), pc.wave.end());
+        TOMO_TRY(wave.ensure(sizeof(Real) * wv.size()));
+        CUDA_TRY(cudaMemcpy(wave.p, wv.data(), sizeof(Real) * wv.size(), cudaMemcpyHostToDevice));
+        TOMO_TRY(rx.ensure(sizeof(int) * std::max<size_t>(pc.rx.size(), 2)));
+        if (!pc.rx.empty()) CUDA_TRY(cudaMemcpy(rx.p, pc.rx.data(), sizeof(int) * pc.rx.size(), cudaMemcpyHostToDevice));
+        if (!pc.patchmap.empty()) {
+            TOMO_TRY(patch.ensure(pc.patchmap.size()));
+            CUDA_TRY(cudaMemcpy(patch.p, pc.patchmap.data(), pc.patchmap.size(), cudaMemcpyHostToDevice));
+        }
+        TOMO_TRY(freqs.ensure(sizeof(double) * TOMO_MAX_FREQS));
+        CUDA_TRY(cudaMemcpy(freqs.p, pc.spec.freqs, sizeof(double) * TOMO_MAX_FREQS, cudaMemcpyHostToDevice));
+        if (pc.C > 0) {
+            TOMO_TRY(ffgeom.ensure(sizeof(double) * pc.ffgeom.size()));
+            CUDA_TRY(cudaMemcpy(ffgeom.p, pc.ffgeom.data(), sizeof(double) * pc.ffgeom.size(), cudaMemcpyHostToDevice));
+        }
+        if (pc.nang > 0) {
+            TOMO_TRY(ffang.ensure(sizeof(double) * pc.ffang.size()));
+            CUDA_TRY(cudaMemcpy(ffang.p, pc.ffang.data(), sizeof(double) * pc.ffang.size(), cudaMemcpyHostToDevice));
+        }
+        return TOMO_OK;
+    }
+
+    size_t target_size() const {
+        return pc.spec.mode == TOMO_MODE_BREAST ? (size_t)pc.n_exc * pc.nrx * pc.S
+                                                : (size_t)pc.n_exc * pc.nfreq * pc.nang;
+    }
+
+    int set_target(const float* t, size_t n) {
+        if (!t || n != target_size())
+            return fail(TOMO_EINVAL, "target has " + std::to_string(n) + " values, expected " + std::to_string(target_size()));
+        TOMO_TRY(target.ensure(sizeof(float) * n));
+        CUDA_TRY(cudaMemcpy(target.p, t, sizeof(float) * n, cudaMemcpyHostToDevice));
+        have_target = true;
+        return TOMO_OK;
+    }
+};
+
+// Upload unpacked arguments and build material maps and FP64-derived
+// coefficient tables for `ncand` candidates.  d_upload must hold
+// u.upload.size() doubles.  Returns the number of kernels launched via *kernels.
+template <typename Real>
+int setup_materials(const ClassData<Real>& cd, const Unpacked& u, double* d_upload, uint8_t* d_mats, Real* d_tabs,
+                    cudaStream_t st, int64_t* kernels, int64_t* h2d) {
+    const tomo_spec& s = cd.pc.spec;
+    const size_t ncand = u.ncand;
+    if (h2d) {   // upload here unless the caller already did
+        CUDA_TRY(cudaMemcpyAsync(d_upload, u.upload.data(), sizeof(double) * u.upload.size(), cudaMemcpyHostToDevice, st));
+        *h2d += sizeof(double) * u.upload.size();
+    }
+    material_table_kernel<Real><<<(int)((ncand * kMaxMat + 127) / 128), 128, 0, st>>>(d_upload, d_tabs, (int)ncand,
+                                                                                     cd.pc.nmat, s.tau, s.dt, s.dx);
+    ++*kernels;
+    if (s.mode == TOMO_MODE_BREAST) {
+        dim3 blk(32, 8), grd((s.nx + 1 + 31) / 32, (s.ny + 1 + 7) / 8, (unsigned)ncand);
+        raster_ellipse_kernel<<<grd, blk, 0, st>>>(d_mats, cd.pc.mpitch, s.nx, s.ny, s.dx, s.disc_radius,
+                                                   d_upload + ncand * kMaxMat * 3, s.n_ellipses, cd.lay.mat_stride);
+        mark_rx_kernel<<<(int)((cd.pc.nrx * ncand + 127) / 128), 128, 0, st>>>(d_mats, cd.pc.mpitch, cd.lay.mat_stride,
+                                                                              cd.rx.template as<int>(), cd.pc.nrx,
+                                                                              (int)ncand);
+        *kernels += 2;
+    }
+    CUDA_TRY(cudaGetLastError());
+    return TOMO_OK;
+}
+
+// Descriptors of the ncand*n_exc solves of a range whose state starts at
+// state_base (per-solve stride cd.lay.per_solve elements).
+template <typename Real>
+void fill_descs(const ClassData<Real>& cd, const Unpacked& u, Real* state_base, const uint8_t* mats, const Real* tabs,
+                SolveDesc<Real>* out) {
+    const ProblemClass& pc = cd.pc;
+    const tomo_spec& s = pc.spec;
+    const SolveLayout& L = cd.lay;
+    const int nsolves = (int)u.ncand * pc.n_exc;
+    for (int sv = 0; sv < nsolves; ++sv) {
+        const int cand = sv / pc.n_exc, exc = sv % pc.n_exc;
+        SolveDesc<Real> D{};
+        Real* sb = state_base + (size_t)sv * L.per_solve;
+        D.nx = s.nx; D.ny = s.ny; D.pitch = pc.pitch; D.mpitch = pc.mpitch;
+        D.ncpml = pc.nc; D.steps_total = pc.S; D.step = 0; D.parity = 0; D.active = 1;
+        D.nrx = pc.nrx; D.nf_d = s.nf2ff_d; D.nfreq = pc.nfreq; D.n_contour = pc.C;
+        D.chez = (Real)pc.chez; D.Kp = (Real)pc.Kp; D.dx = (Real)s.dx;
+        Real* f = sb + kPadLeft;
+        D.ez[0] = f + 0 * L.field_elems; D.ez[1] = f + 1 * L.field_elems;
+        D.hx[0] = f + 2 * L.field_elems; D.hx[1] = f + 3 * L.field_elems;
+        D.hy[0] = f + 4 * L.field_elems; D.hy[1] = f + 5 * L.field_elems;
+        D.jp[0] = f + 6 * L.field_elems; D.jp[1] = f + 7 * L.field_elems;
+        Real* psib = sb + 8 * L.field_elems;
+        D.psi[0] = psib;
+        D.psi[1] = psib + L.psi_elems;
+        D.psi_scratch = psib + 2 * L.psi_elems;
+        D.psi_stride = (int)L.psi_elems;
+        D.traces = psib + (size_t)9 * L.psi_elems;
+        D.acc = D.traces + L.tr_stride;
+        D.mtab = tabs + (size_t)cand * kMaxMat * kMatCoef;
+        D.cpml = cd.cpml.template as<Real>();
+        D.src_wave = cd.wave.template as<Real>();
+        D.rx = cd.rx.template as<int>();
+        D.phasor = cd.phasor.template as<Real>();
+        const int* bb = &u.bbox[cand * 4];
+        D.jx0 = bb[0]; D.jx1 = bb[1]; D.jy0 = bb[2]; D.jy1 = bb[3];
+        D.dt = s.dt;
+        if (s.mode == TOMO_MODE_BREAST) {
+            D.flags = kPointSource;
+            D.mat = mats + (size_t)cand * L.mat_stride + kMatPadLeft;
+            D.src_x = pc.rx[2 * exc];
+            D.src_y = pc.rx[2 * exc + 1];
+        } else {
+            D.flags = kRefCpml | kPlaneWave | (s.nan_clamp ? kNanClamp : 0);
+            D.mat = cd.patch.template as<uint8_t>() + kMatPadLeft;
+            D.src_x = D.src_y = -1;
+            // fwf() (FDTD_GPU.cu:283-296): the excitation angle is a float in the reference
+            const float phi = (float)(exc * 2 * kPiD / s.n_excitations);
+            D.pw_kx = std::cos((double)phi);
+            D.pw_ky = std::sin((double)phi);
+            D.pw_xoff = s.pw_centred ? (double)(s.nx / 2) : 0.0;
+            D.pw_yoff = s.pw_centred ? (double)(s.ny / 2) : 0.0;
+            D.pw_t0l = s.pw_t0 - s.pw_l / kC0;
+            D.pw_inv_tau = 1.0 / s.pw_tau;
+            D.pw_dxc0 = s.dx / kC0;
+        }
+        out[sv] = D;
+    }
+}
+
+// Far field + misfit (+ optional traces to float) of a contiguous range of
+// solves whose first descriptor is `first` (host copy).  d_D/d_P hold
+// nsolves*nfreq*nang floats; d_fit receives ncand values.
+template <typename Real>
+int post_range(const ClassData<Real>& cd, size_t ncand, const SolveDesc<Real>& first, bool want_fit, float* d_D,
+               float* d_P, double* d_partials, double* d_fit, int* d_flag, float* d_trf, double* d_trd, cudaStream_t st,
+               int64_t* kernels) {
+    const ProblemClass& pc = cd.pc;
+    const tomo_spec& s = pc.spec;
+    const int nsolves = (int)ncand * pc.n_exc;
+    const size_t stride = cd.lay.per_solve;
+    if (pc.nang > 0 && pc.C > 0 && d_D) {
+        dim3 grd(pc.nfreq, nsolves);
+        farfield_kernel<Real><<<grd, 256, 0, st>>>(first.acc, stride, pc.C, pc.nfreq, cd.freqs.template as<double>(),
+                                                   cd.ffgeom.template as<double>(), cd.ffang.template as<double>(),
+                                                   pc.nang, s.dx, s.ff_norm, s.pw_tau, d_D, d_P);
+        ++*kernels;
+    }
+    if (want_fit) {
+        if (s.mode == TOMO_MODE_BREAST) {
+            trace_partials_kernel<Real><<<nsolves, 256, 0, st>>>(first.traces, stride, cd.target.template as<float>(),
+                                                                 pc.nrx * pc.S, pc.n_exc, 0, d_partials, d_flag);
+            trace_fitness_kernel<<<(int)((ncand + 127) / 128), 128, 0, st>>>(d_partials, pc.n_exc, (int)ncand, d_fit);
+            *kernels += 2;
+        } else {
+            const int nper = pc.n_exc * pc.nfreq * pc.nang;
+            ff_fitness_kernel<<<(int)ncand, 256, 0, st>>>(d_D, cd.target.template as<float>(), nper,
+                                                          (double)pc.n_exc * pc.nfreq, s.misfit == 1, d_fit, d_flag);
+            ++*kernels;
+        }
+    }
+    if ((d_trf || d_trd) && pc.nrx > 0) {
+        const size_t n = (size_t)pc.nrx * pc.S * nsolves;
+        if (d_trf)
+            traces_pack_kernel<Real, float><<<(int)((n + 255) / 256), 256, 0, st>>>(first.traces, stride, pc.nrx * pc.S,
+                                                                                    nsolves, d_trf);
+        if (d_trd)
+            traces_pack_kernel<Real, double><<<(int)((n + 255) / 256), 256, 0, st>>>(first.traces, stride, pc.nrx * pc.S,
+                                                                                     nsolves, d_trd);
+        *kernels += (d_trf ? 1 : 0) + (d_trd ? 1 : 0);
+    }
+    CUDA_TRY(cudaGetLastError());
+    return TOMO_OK;
+}
+
+// Grid size of the persistent advance kernel.
+template <typename Real>
+int advance_grid(int T, int cols, int mode, int nitems, int num_sms, int* blocks, size_t* smem) {
+    AdvanceFn<Real> fn = advance_kernel_for<Real>(T, cols, mode);
+    if (!fn) return fail(TOMO_EINVAL, "unsupported (steps_per_launch, cols_per_lane) pair");
+    *smem = advance_smem_bytes<Real>(T, cols);
+    CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem));
+    int per_sm = 0;
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 128, *smem));
+    per_sm = std::max(per_sm, 1);
+    *blocks = std::max(1, std::min((nitems + 3) / 4, num_sms * per_sm));
+    return TOMO_OK;
+}
+
+template <typename Real>
+void launch_advance(int T, int cols, int mode, int blocks, size_t smem, const SolveDesc<Real>* descs,
+                    const WorkItem* items, int nitems, int nsolves, cudaStream_t st) {
+    AdvanceFn<Real> fn = advance_kernel_for<Real>(T, cols, mode);
+    fn<<<blocks, 128, smem, st>>>(descs, items, nitems);
+    bump_kernel<Real><<<(nsolves + 127) / 128, 128, 0, st>>>(const_cast<SolveDesc<Real>*>(descs), nsolves, T);
+}
+
+// Work items (solve, strip) for nsolves solves starting at solve index first.
+inline void append_items(std::vector<WorkItem>& items, int first, int nsolves, int nx, int T, int cols) {
+    const int W = 32 * cols - 2 * T;
+    const int nstrips = (nx + 1 + W - 1) / W;
+    for (int sv = 0; sv < nsolves; ++sv)
+        for (int q = 0; q < nstrips; ++q) items.push_back({first + sv, q});
+}
+
+// ------------------------------------------------------------------- engine
+template <typename Real>
+struct ServeStateT;
+
+template <typename Real>
+class EngineT : public EngineBase {
+   public:
+    EngineT() = default;
+    ~EngineT() override;
+    int init(const ProblemClass& pc);
+    int set_stream(void* s) override;
+    int set_budget(uint64_t b) override;
+    int set_target(const float* t, size_t n) override { return cd_.set_target(t, n); }
+    int stats(tomo_stats* st) override {
+        if (!st) return fail(TOMO_EINVAL, "stats is NULL");
+        *st = stats_;
+        return TOMO_OK;
+    }
+    int forward(const double* args, size_t ncand, size_t nparam, const tomo_outputs* out) override;
+    // serving (serve.cu)
+    int submit(const double* args, size_t ncand, size_t nparam, uint64_t* ticket) override;
+    int submit_spec(const tomo_spec* spec, const double* args, size_t ncand, size_t nparam, uint64_t* ticket) override;
+    int set_target_spec(const tomo_spec* spec, const float* t, size_t n) override;
+    int serve_step(int* n_active) override;
+    int poll(uint64_t ticket, double* fitness) override;
+    int cancel(uint64_t ticket) override;
+
+   private:
+    int ensure_batch(int ncand);
+    int build_graph(int nlaunch);
+    void invalidate_graph() {
+        if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+        graph_exec_ = nullptr;
+    }
+    void serve_release();
+    ClassData<Real>* class_for(const tomo_spec* spec, int* rc);
+
+    ClassData<Real> cd_;
+    cudaStream_t stream_ = nullptr;
+    bool own_stream_ = false;
+    cudaEvent_t ev_[4] = {nullptr, nullptr, nullptr, nullptr};
+    int num_sms_ = 0;
+    int T_ = 1, cols_ = 1;
+    uint64_t budget_ = (uint64_t)150 << 30;
+    tomo_stats stats_{};
+    // batch buffers
+    int cap_cand_ = 0, cur_cand_ = 0, nsolves_ = 0, nitems_ = 0;
+    DevBuf d_state_, d_mats_, d_tabs_, d_upload_, d_descs_, d_items_, d_partials_, d_fit_, d_D_, d_P_, d_flag_, d_trf_,
+        d_trd_;
+    Unpacked up_;
+    std::vector<SolveDesc<Real>> h_descs_;
+    cudaGraphExec_t graph_exec_ = nullptr;
+    int graph_cand_ = -1, graph_T_ = -1, graph_cols_ = -1, graph_launches_ = -1, graph_blocks_ = 0;
+    // serving
+    ServeStateT<Real>* serve_ = nullptr;
+};
+
+}  // namespace tomo

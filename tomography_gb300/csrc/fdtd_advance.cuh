@@ -1,0 +1,683 @@
+// Wavefront temporal-blocking FDTD advance kernel (2D TMz Yee + CPML + Debye ADE).
+//
+// Work decomposition.  A work item is one vertical strip of one solve.  One
+// warp owns the item: each lane holds COLS consecutive columns, so a warp
+// spans P = 32*COLS columns, of which the middle W = P - 2T are written back
+// (the T columns on either side are a recomputed halo).  The warp sweeps the
+// strip bottom-to-top, one row per iteration, and carries T time levels in
+// flight: level k receives row r-2k (from level k-1 one iteration earlier),
+// advances row r-2k-1 from time n0+k to n0+k+1 and hands it to level k+1.
+// Every row is therefore read from HBM once and written once per T time
+// steps; x-neighbours come from warp shuffles, y-neighbours from registers.
+// Levels are processed in descending order so that no level waits on another
+// inside an iteration (independent instruction streams for the scheduler).
+//
+// Two code paths per (row, level), chosen warp-uniformly:
+//  * fast path: interior rows of interior strips (no CPML, no boundary, no
+//    NTFF face, no source or receiver, no plane-wave cell) -- the plain Yee +
+//    Debye update;
+//  * general path: everything else.
+// Both evaluate the same explicitly rounded formulas, so a cell gives the
+// same bits whichever path computes it.
+//
+// Physics per cell follows the reference kernels:
+//   H update  FDTD_GPU.cu:298-355  (Hy += Chez dEz/dx, Hx -= Chez dEz/dy, CPML psi)
+//   E update  FDTD_GPU.cu:358-434  (Ceze, Cezh, Debye polarisation current Jp,
+//             scattered-field plane wave, CPML psi; PEC boundary)
+//   DFT       FDTD_GPU.cu:231-280  (running DFT of J = n x H and M = -n x E on
+//             the NTFF rectangle; contour order of FDTD_common.cxx:4-46)
+// extended with a soft point current source (FDTD_CPU.cxx:324-327, 972-983)
+// and receiver sampling (FDTD_CPU.cxx:808).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "solve_desc.h"
+
+namespace tomo {
+
+struct WorkItem {
+    int solve;
+    int strip;
+};
+
+enum AdvanceMode : int {
+    kModeBreast = 0,   // proper CPML, point current source, no plane wave
+    kModeRef = 1       // reference CPML semantics, scattered-field plane wave, optional NaN clamp
+};
+
+constexpr int kMaxRowWords = 256;   // row-flag words per warp: grids up to 8192 rows
+
+template <typename Real>
+__device__ __forceinline__ Real dev_exp(Real v);
+template <>
+__device__ __forceinline__ float dev_exp<float>(float v) { return expf(v); }
+template <>
+__device__ __forceinline__ double dev_exp<double>(double v) { return exp(v); }
+
+template <typename Real>
+__device__ __forceinline__ bool dev_isnan(Real v) { return v != v; }
+
+// Explicitly rounded arithmetic: the update formulas are written with these so
+// that no instantiation (blocking depth, columns per lane, code path, register
+// pressure) can contract them differently -- every configuration gives
+// bit-identical fields.
+template <typename Real>
+struct Op;
+template <>
+struct Op<float> {
+    static __device__ __forceinline__ float fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+    static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+    static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+};
+template <>
+struct Op<double> {
+    static __device__ __forceinline__ double fma(double a, double b, double c) { return __fma_rn(a, b, c); }
+    static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+    static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+    static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+};
+
+// Asynchronous global->shared copies (cp.async, completion per thread via
+// commit/wait groups).  src_bytes = 0 zero-fills without reading global memory.
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* smem_dst, const void* gmem_src, bool valid) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    const int n = valid ? BYTES : 0;
+    if constexpr (BYTES == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(gmem_src), "r"(n) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(d), "l"(gmem_src), "n"(BYTES), "r"(n)
+                     : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+constexpr int kPrefetch = 7;       // rows in flight ahead of the one being consumed
+constexpr int kRowSlots = 8;       // ring slots per warp (kPrefetch + 1)
+
+// Kahan-compensated accumulation (FP32); plain accumulation in FP64.
+template <typename Real>
+__device__ __forceinline__ void acc_add(Real& sum, Real& comp, Real term) {
+    using O = Op<Real>;
+    Real y = O::sub(term, comp);
+    Real t = O::add(sum, y);
+    comp = O::sub(O::sub(t, sum), y);
+    sum = t;
+}
+template <>
+__device__ __forceinline__ void acc_add<double>(double& sum, double& comp, double term) {
+    (void)comp;
+    sum = __dadd_rn(sum, term);
+}
+
+// Contour index of a cell on a face (inverse of FDTD_common.cxx:4-46).
+__device__ __forceinline__ int contour_index_yn(int nx, int ny, int d, int x) { return x - d - 1; }
+__device__ __forceinline__ int contour_index_yp(int nx, int ny, int d, int x) {
+    int l1 = nx - 2 * d - 2, l2 = l1 + (ny - 2 * d);
+    return l2 + (nx - d - 2 - x);
+}
+__device__ __forceinline__ int contour_index_xp(int nx, int ny, int d, int y) { return (nx - 2 * d - 2) + (y - d); }
+__device__ __forceinline__ int contour_index_xn(int nx, int ny, int d, int y) {
+    int l1 = nx - 2 * d - 2, l3 = 2 * l1 + (ny - 2 * d);
+    return l3 + (ny - d - 1 - y);
+}
+
+// One running-DFT update of one contour cell (J from h, M from the face-averaged e).
+template <typename Real>
+__device__ __forceinline__ void dft_update(Real* acc, const Real* ph, int nfreq, int C, int c, Real h, Real e) {
+    for (int f = 0; f < nfreq; ++f) {
+        const Real* p = ph + 4 * f;
+        Real* a = acc + ((size_t)f * C + c) * 8;
+        Real s0 = a[0], s1 = a[1], c0 = a[2], c1 = a[3], s2 = a[4], s3 = a[5], c2 = a[6], c3 = a[7];
+        acc_add(s0, c0, Op<Real>::mul(h, p[0]));
+        acc_add(s1, c1, Op<Real>::mul(h, p[1]));
+        acc_add(s2, c2, Op<Real>::mul(e, p[2]));
+        acc_add(s3, c3, Op<Real>::mul(e, p[3]));
+        a[0] = s0; a[1] = s1; a[2] = c0; a[3] = c1; a[4] = s2; a[5] = s3; a[6] = c2; a[7] = c3;
+    }
+}
+
+// Dynamic shared memory per block (4 warps).
+template <typename Real, int T, int COLS>
+struct AdvanceSmem {
+    Real rows[4][kRowSlots][4][32 * COLS];   // per-warp prefetch ring: Ez, Hx, Hy, Jp of kRowSlots rows
+    Real tab[4][kMaxMat][4];                 // per-warp Ca, Cb, Cj, Bp of every material
+    Real ring[4][2][kRing][T][2];            // per-warp vertical-face DFT samples (h, e)
+    uint32_t rowbits[4][kMaxRowWords];       // per-warp "row needs the general path" flags
+    uint8_t mats[4][kRowSlots][32 * COLS + 16];   // per-warp prefetch ring: material bytes
+};
+
+template <typename Real, int T, int COLS, int MODE>
+__device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, AdvanceSmem<Real, T, COLS>& sm,
+                             int wib) {
+    // The descriptor is read-only for the whole launch (restrict).
+    const SolveDesc<Real>& D = *Dp;
+    using O = Op<Real>;
+    constexpr int P = 32 * COLS;
+    constexpr int W = P - 2 * T;
+    constexpr bool kRef = MODE == kModeRef;
+    const int lane = threadIdx.x & 31;
+    const int nx = D.nx, ny = D.ny, nc = D.ncpml, S = D.steps_total, n0 = D.step;
+    const int nsteps = min(T, S - n0);
+    if (nsteps <= 0) return;
+    const int pitch = D.pitch;
+    const int xs = strip * W - T;      // column of position 0
+    const int src = D.parity, dst = 1 - src;
+    const Real chez = D.chez, Kp = D.Kp, dxr = D.dx;
+    const bool clampnan = kRef && (D.flags & kNanClamp) != 0;
+    const bool psrc = !kRef && (D.flags & kPointSource) != 0;
+    const int C = D.n_contour, nfreq = D.nfreq, fd = D.nf_d;
+    const int psx_h = 0, psx_e = (ny + 1) * 2 * nc;                 // x-strip psi sub-arrays
+    const int psy0 = 2 * (ny + 1) * 2 * nc;
+    const int psy_h = psy0, psy_e = psy0 + 2 * nc * (nx + 1);         // y-strip psi sub-arrays
+    const uint8_t* __restrict__ matp = D.mat;
+    const Real* __restrict__ cpml = D.cpml;
+    const Real* __restrict__ phasor = D.phasor;
+    Real* __restrict__ acc = D.acc;
+    const int mpitch = D.mpitch, jx0 = D.jx0, jx1 = D.jx1, jy0 = D.jy0, jy1 = D.jy1;
+    const int src_x = D.src_x, src_y = D.src_y;
+
+    // hot material coefficients -> shared memory (per warp)
+    for (int i = lane; i < kMaxMat * 4; i += 32) sm.tab[wib][i >> 2][i & 3] = D.mtab[(i >> 2) * kMatCoef + (i & 3)];
+
+    // per-column constants
+    int xcol[COLS];
+    int ixh[COLS], ixe[COLS];
+    bool owned[COLS];
+    int face_slot[COLS];   // 0: xn face column, 1: xp face column, -1 none
+    bool wspecial = false, wdisp = false;
+#pragma unroll
+    for (int c = 0; c < COLS; ++c) {
+        int x = xs + lane * COLS + c;
+        xcol[c] = x;
+        int pos = lane * COLS + c;
+        owned[c] = pos >= T && pos < P - T && x >= 0 && x <= nx;
+        ixh[c] = (x >= 0 && x < nc) ? nc - 1 - x : ((x >= nx - nc && x < nx) ? x - nx + nc : -1);
+        ixe[c] = (x >= 1 && x <= nc) ? nc - x : ((x >= nx - nc && x <= nx - 1) ? x - nx + nc : -1);
+        face_slot[c] = -1;
+        if (nfreq > 0 && owned[c]) {
+            if (x == fd) face_slot[c] = 0;
+            else if (x == nx - fd - 1) face_slot[c] = 1;
+        }
+        // CPML strips, PEC boundary and padding columns, vertical NTFF faces
+        wspecial |= x <= nc || x >= nx - nc || (nfreq > 0 && (x == fd || x == nx - fd - 1));
+        wdisp |= x >= jx0 && x <= jx1;
+    }
+    bool has_face0 = false, has_face1 = false;
+#pragma unroll
+    for (int c = 0; c < COLS; ++c) {
+        has_face0 |= face_slot[c] == 0;
+        has_face1 |= face_slot[c] == 1;
+    }
+    has_face0 = __any_sync(0xffffffffu, has_face0);
+    has_face1 = __any_sync(0xffffffffu, has_face1);
+    wspecial = __any_sync(0xffffffffu, wspecial);
+    wdisp = __any_sync(0xffffffffu, wdisp);
+
+    // rows that need the general path: CPML rows and boundaries, NTFF face rows,
+    // the source row, receiver rows, plane-wave rows (reference modes)
+    uint32_t* rowbits = sm.rowbits[wib];
+    const int nwords = (ny + 1 + 31) >> 5;
+    for (int w = lane; w < nwords; w += 32) {
+        uint32_t bits = 0;
+        for (int b = 0; b < 32; ++b) {
+            const int m = 32 * w + b;
+            bool sp = m <= nc || m >= ny - nc;
+            sp |= nfreq > 0 && (m == fd + 1 || m == ny - fd);
+            sp |= psrc && m == src_y;
+            sp |= kRef && wdisp && m >= jy0 && m <= jy1;
+            if (sp) bits |= 1u << b;
+        }
+        rowbits[w] = bits;
+    }
+    __syncwarp();
+    for (int rr = lane; rr < D.nrx; rr += 32) {
+        const int m = D.rx[2 * rr + 1];
+        atomicOr(&rowbits[m >> 5], 1u << (m & 31));
+    }
+    __syncwarp();
+
+    // level registers
+    Real pz[T][COLS], px_[T][COLS], py_[T][COLS], pj[T][COLS];   // row m input (prev)
+    Real hz[T][COLS], hxr[T][COLS], hyr[T][COLS], hj[T][COLS];   // row m+1 input (handoff)
+    Real hxn[T][COLS], ezn[T][COLS];                             // outputs of row m-1
+    uint32_t pmat[T], hmat[T];                                   // material bytes of those rows, packed
+#pragma unroll
+    for (int k = 0; k < T; ++k) {
+        pmat[k] = hmat[k] = 0u;
+#pragma unroll
+        for (int c = 0; c < COLS; ++c) {
+            pz[k][c] = px_[k][c] = py_[k][c] = pj[k][c] = Real(0);
+            hz[k][c] = hxr[k][c] = hyr[k][c] = hj[k][c] = Real(0);
+            hxn[k][c] = ezn[k][c] = Real(0);
+        }
+    }
+
+    const Real* __restrict__ ez_s = D.ez[src];
+    const Real* __restrict__ hx_s = D.hx[src];
+    const Real* __restrict__ hy_s = D.hy[src];
+    const Real* __restrict__ jp_s = D.jp[src];
+    Real* __restrict__ ez_d = D.ez[dst];
+    Real* __restrict__ hx_d = D.hx[dst];
+    Real* __restrict__ hy_d = D.hy[dst];
+    Real* __restrict__ jp_d = D.jp[dst];
+    auto psi_copy = [&](int level) -> Real* {
+        // time copy holding psi at time n0+level
+        if (level == 0) return D.psi[src];
+        if (level == T) return D.psi[dst];
+        return D.psi_scratch + (size_t)(level - 1) * D.psi_stride;
+    };
+
+    // Rows stream through a per-warp shared-memory ring: row r + kPrefetch is
+    // requested (cp.async) while row r is consumed, so kPrefetch rows of every
+    // warp are in flight and HBM latency is hidden.  Each lane copies its own
+    // columns of the four fields; lanes 0..P/4 copy the material bytes.
+    constexpr int kBytes = COLS * (int)sizeof(Real);
+    const int mstart = xs & ~3;        // 4-byte aligned start of the material window
+    const int moff = xs - mstart;
+    auto issue_row = [&](int r) {
+        const int slot = r & (kRowSlots - 1);
+        const bool valid = r <= ny;
+        const long long rowoff = (long long)(valid ? r : 0) * pitch;
+        const int x0 = xs + lane * COLS;
+        Real* d = &sm.rows[wib][slot][0][lane * COLS];
+        cp_async<kBytes>(d, ez_s + rowoff + x0, valid);
+        cp_async<kBytes>(d + P, hx_s + rowoff + x0, valid);
+        cp_async<kBytes>(d + 2 * P, hy_s + rowoff + x0, valid);
+        const bool jv = valid && r >= jy0 && r <= jy1 && x0 + COLS - 1 >= jx0 && x0 <= jx1;
+        cp_async<kBytes>(d + 3 * P, jp_s + rowoff + x0, jv);
+        if (lane <= P / 4)
+            cp_async<4>(&sm.mats[wib][slot][4 * lane], matp + (long long)(valid ? r : 0) * mpitch + mstart + 4 * lane,
+                        valid);
+        cp_async_commit();
+    };
+#pragma unroll 1
+    for (int r = 0; r < kPrefetch; ++r) issue_row(r);
+
+    const int rmax = ny + 2 * T - 1;
+    int flushed = 0;   // next face row not yet flushed
+    for (int r = 0; r <= rmax; ++r) {
+        // ---- level 0 input: row r from the ring; request row r + kPrefetch
+        cp_async_wait<kPrefetch - 1>();
+        __syncwarp();
+        Real lz[COLS], lx[COLS], ly[COLS], lj[COLS];
+        uint32_t lm = 0u;
+        {
+            const int slot = r & (kRowSlots - 1);
+            const Real* sp = &sm.rows[wib][slot][0][lane * COLS];
+#pragma unroll
+            for (int c = 0; c < COLS; ++c) {
+                lz[c] = sp[c];
+                lx[c] = sp[P + c];
+                ly[c] = sp[2 * P + c];
+                lj[c] = sp[3 * P + c];
+                lm |= (uint32_t)sm.mats[wib][slot][moff + lane * COLS + c] << (8 * c);
+            }
+        }
+        issue_row(r + kPrefetch);
+
+#pragma unroll
+        for (int k = T - 1; k >= 0; --k) {
+            const int q = r - 2 * k;       // row received this iteration
+            const int m = q - 1;           // row advanced this iteration
+            Real iz[COLS], ix[COLS], iy[COLS], ij[COLS];
+            const uint32_t im = (k == 0) ? lm : hmat[k];
+#pragma unroll
+            for (int c = 0; c < COLS; ++c) {
+                if (k == 0) { iz[c] = lz[c]; ix[c] = lx[c]; iy[c] = ly[c]; ij[c] = lj[c]; }
+                else { iz[c] = hz[k][c]; ix[c] = hxr[k][c]; iy[c] = hyr[k][c]; ij[c] = hj[k][c]; }
+            }
+            if (q < 0 || m > ny) continue;   // level idle (uniform)
+            if (m >= 0) {
+                Real oz[COLS], ox[COLS], oy[COLS], oj[COLS];
+                const int n = n0 + k;        // time step index computed by this level
+                const bool fast = !wspecial && !((rowbits[m >> 5] >> (m & 31)) & 1u);
+                if (k < nsteps && fast) {
+                    // ================= fast path: interior Yee + Debye
+                    const Real ezR_last = __shfl_down_sync(0xffffffffu, pz[k][0], 1);
+#pragma unroll
+                    for (int c = 0; c < COLS; ++c) {
+                        const Real ez0 = pz[k][c];
+                        const Real ezR = (c + 1 < COLS) ? pz[k][c + 1] : ezR_last;
+                        oy[c] = O::fma(chez, O::sub(ezR, ez0), py_[k][c]);
+                        ox[c] = O::fma(-chez, O::sub(iz[c], ez0), px_[k][c]);
+                        if (clampnan) {
+                            if (dev_isnan(ox[c])) ox[c] = Real(0);
+                            if (dev_isnan(oy[c])) oy[c] = Real(0);
+                        }
+                    }
+                    const Real hyL_first = __shfl_up_sync(0xffffffffu, oy[COLS - 1], 1);
+#pragma unroll
+                    for (int c = 0; c < COLS; ++c) {
+                        const int mi = (pmat[k] >> (8 * c)) & kMatMask;
+                        const Real Ca = sm.tab[wib][mi][kCa], Cb = sm.tab[wib][mi][kCb];
+                        const Real Cj = sm.tab[wib][mi][kCj], Bp = sm.tab[wib][mi][kBp];
+                        const Real hyL = (c > 0) ? oy[c - 1] : hyL_first;
+                        const Real dHy = O::sub(oy[c], hyL);
+                        const Real dHx = O::sub(ox[c], hxn[k][c]);
+                        const Real ez = pz[k][c], jp = pj[k][c];
+                        Real out;
+                        if (kRef) out = O::fma(Ca, ez, O::sub(O::mul(Cb, dHy), O::mul(Cb, dHx)));
+                        else out = O::fma(Ca, ez, O::mul(Cb, O::sub(dHy, dHx)));
+                        out = O::fma(-Cj, jp, out);
+                        oj[c] = O::fma(Kp, jp, O::mul(Bp, O::sub(out, ez)));
+                        if (clampnan && dev_isnan(out)) out = Real(0);
+                        oz[c] = out;
+                    }
+                } else if (k < nsteps) {
+                    // ================= general path
+                    const bool hrow = m < ny;
+                    const int iyh = (m < nc) ? nc - 1 - m : ((m >= ny - nc && m < ny) ? m - ny + nc : -1);
+                    Real ezR_last = __shfl_down_sync(0xffffffffu, pz[k][0], 1);
+#pragma unroll
+                    for (int c = 0; c < COLS; ++c) {
+                        const int x = xcol[c];
+                        Real ez0 = pz[k][c];
+                        Real ezR = (c + 1 < COLS) ? pz[k][c + 1] : ezR_last;
+                        Real hx0 = px_[k][c], hy0 = py_[k][c];
+                        Real hx = hx0, hy = hy0;
+                        const int pos = lane * COLS + c;
+                        const bool hvalid = pos >= k && pos <= P - 2 - k;
+                        if (hrow && x >= 0 && x < nx) {
+                            Real dEy = O::sub(ezR, ez0);
+                            Real dEx = O::sub(iz[c], ez0);
+                            hy = O::fma(chez, dEy, hy0);
+                            hx = O::fma(-chez, dEx, hx0);
+                            if (ixh[c] >= 0) {
+                                const int i = ixh[c];
+                                const int xsx = (x < nc) ? x : x - (nx - nc) + nc;
+                                Real* pin = psi_copy(k) + psx_h + (size_t)m * 2 * nc + xsx;
+                                Real* pout = psi_copy(k + 1) + psx_h + (size_t)m * 2 * nc + xsx;
+                                Real ps = O::fma(cpml[4 * nc + i], *pin, O::mul(cpml[5 * nc + i], dEy));
+                                if (hvalid) *pout = ps;
+                                hy = O::fma(O::mul(chez, dEy), cpml[3 * nc + i], hy0);
+                                hy = O::fma(O::mul(chez, dxr), ps, hy);
+                            }
+                            if (iyh >= 0) {
+                                const int ysx = (m < nc) ? m : m - (ny - nc) + nc;
+                                Real* pin = psi_copy(k) + psy_h + (size_t)ysx * (nx + 1) + x;
+                                Real* pout = psi_copy(k + 1) + psy_h + (size_t)ysx * (nx + 1) + x;
+                                Real ps = O::fma(cpml[4 * nc + iyh], *pin, O::mul(cpml[5 * nc + iyh], dEx));
+                                if (hvalid) *pout = ps;
+                                hx = O::fma(-O::mul(chez, dEx), cpml[3 * nc + iyh], hx0);
+                                hx = O::fma(-O::mul(chez, dxr), ps, hx);
+                            }
+                            if (clampnan) {
+                                if (dev_isnan(hx)) hx = Real(0);
+                                if (dev_isnan(hy)) hy = Real(0);
+                            }
+                        }
+                        ox[c] = hx;
+                        oy[c] = hy;
+                    }
+                    Real hyL_first = __shfl_up_sync(0xffffffffu, oy[COLS - 1], 1);
+                    const bool erow = m >= 1 && m <= ny - 1;
+                    const int iye = (m >= 1 && m <= nc) ? nc - m : ((m >= ny - nc && m <= ny - 1) ? m - ny + nc : -1);
+#pragma unroll
+                    for (int c = 0; c < COLS; ++c) {
+                        const int x = xcol[c];
+                        const int pos = lane * COLS + c;
+                        const bool evalid = pos >= k + 1 && pos <= P - 2 - k;
+                        Real ez = pz[k][c];
+                        Real jp = pj[k][c];
+                        Real out = Real(0);
+                        Real jpo = jp;
+                        if (erow && x >= 1 && x <= nx - 1) {
+                            const uint32_t mb = (pmat[k] >> (8 * c)) & 0xffu;
+                            const int mi = mb & kMatMask;
+                            const Real* cf = D.mtab + mi * kMatCoef;     // cold columns (global, cached)
+                            const Real Ca = sm.tab[wib][mi][kCa], Cb = sm.tab[wib][mi][kCb];
+                            const Real Cj = sm.tab[wib][mi][kCj], Bp = sm.tab[wib][mi][kBp];
+                            Real hyL = (c > 0) ? oy[c - 1] : hyL_first;
+                            Real dHy = O::sub(oy[c], hyL);
+                            Real dHx = O::sub(ox[c], hxn[k][c]);
+                            Real gp = Real(0), gm = Real(0);
+                            if (kRef) {
+                                const Real Ci = cf[kCi], Cp = cf[kCp];
+                                if (Ci != Real(0) || Cp != Real(0) || Bp != Real(0)) {
+                                    // fwf() argument in FP64 (FDTD_GPU.cu:290): time minus the
+                                    // projected travel time of the incident front to this cell
+                                    const double b = __dmul_rn(__dadd_rn(__dmul_rn(D.pw_ky, (double)m - D.pw_yoff),
+                                                                         __dmul_rn(D.pw_kx, (double)x - D.pw_xoff)),
+                                                               D.pw_dxc0);
+                                    const double a0 = __dsub_rn(__dsub_rn(__dmul_rn((double)n + 0.5, D.dt), D.pw_t0l), b);
+                                    const double a1 = __dsub_rn(__dsub_rn(__dmul_rn((double)n - 0.5, D.dt), D.pw_t0l), b);
+                                    Real u0 = (Real)__dmul_rn(a0, D.pw_inv_tau), u1 = (Real)__dmul_rn(a1, D.pw_inv_tau);
+                                    gp = dev_exp<Real>(-O::mul(u0, u0));
+                                    gm = dev_exp<Real>(-O::mul(u1, u1));
+                                }
+                                // FDTD_GPU.cu:378-385 (interior), then the strip overrides :389-416
+                                out = O::fma(Ca, ez, O::sub(O::mul(Cb, dHy), O::mul(Cb, dHx)));
+                                out = O::fma(cf[kCi], gp, O::fma(cf[kCp], gm, out));
+                                out = O::fma(-Cj, jp, out);
+                                jpo = O::fma(Kp, jp, O::mul(Bp, O::add(O::sub(out, ez), O::sub(gp, gm))));
+                                if (ixe[c] >= 0) {
+                                    const int i = ixe[c];
+                                    const int xsx = (x <= nc) ? x - 1 : x - (nx - nc) + nc;
+                                    Real* pin = psi_copy(k) + psx_e + (size_t)m * 2 * nc + xsx;
+                                    Real* pout = psi_copy(k + 1) + psx_e + (size_t)m * 2 * nc + xsx;
+                                    Real ps = O::fma(cpml[nc + i], *pin, O::mul(cpml[2 * nc + i], dHy));
+                                    if (evalid) *pout = ps;
+                                    const Real rk = cpml[i];
+                                    out = O::fma(Ca, ez, O::mul(O::mul(Cb, O::sub(dHy, dHx)), rk));
+                                    out = O::fma(O::mul(Cb, dxr), ps, out);
+                                }
+                                if (iye >= 0) {
+                                    const int ysx = (m <= nc) ? m - 1 : m - (ny - nc) + nc;
+                                    Real* pin = psi_copy(k) + psy_e + (size_t)ysx * (nx + 1) + x;
+                                    Real* pout = psi_copy(k + 1) + psy_e + (size_t)ysx * (nx + 1) + x;
+                                    Real ps = O::fma(cpml[nc + iye], *pin, O::mul(cpml[2 * nc + iye], dHx));
+                                    if (evalid) *pout = ps;
+                                    const Real rk = cpml[iye];
+                                    out = O::fma(Ca, ez, O::mul(O::mul(Cb, O::sub(dHy, dHx)), rk));
+                                    out = O::fma(-O::mul(Cb, dxr), ps, out);
+                                }
+                            } else {
+                                Real cx = dHy, cy = dHx, qx = Real(0), qy = Real(0);
+                                if (ixe[c] >= 0) {
+                                    const int i = ixe[c];
+                                    const int xsx = (x <= nc) ? x - 1 : x - (nx - nc) + nc;
+                                    Real* pin = psi_copy(k) + psx_e + (size_t)m * 2 * nc + xsx;
+                                    Real* pout = psi_copy(k + 1) + psx_e + (size_t)m * 2 * nc + xsx;
+                                    qx = O::fma(cpml[nc + i], *pin, O::mul(cpml[2 * nc + i], dHy));
+                                    if (evalid) *pout = qx;
+                                    cx = O::mul(dHy, cpml[i]);
+                                }
+                                if (iye >= 0) {
+                                    const int ysx = (m <= nc) ? m - 1 : m - (ny - nc) + nc;
+                                    Real* pin = psi_copy(k) + psy_e + (size_t)ysx * (nx + 1) + x;
+                                    Real* pout = psi_copy(k + 1) + psy_e + (size_t)ysx * (nx + 1) + x;
+                                    qy = O::fma(cpml[nc + iye], *pin, O::mul(cpml[2 * nc + iye], dHx));
+                                    if (evalid) *pout = qy;
+                                    cy = O::mul(dHx, cpml[iye]);
+                                }
+                                // proper CPML: both stretched derivatives and both psi terms
+                                if (ixe[c] >= 0 || iye >= 0)
+                                    out = O::fma(Ca, ez, O::mul(Cb, O::fma(dxr, O::sub(qx, qy), O::sub(cx, cy))));
+                                else
+                                    out = O::fma(Ca, ez, O::mul(Cb, O::sub(dHy, dHx)));
+                                out = O::fma(-Cj, jp, out);
+                                if (psrc && m == src_y && x == src_x) out = O::fma(cf[kCs], D.src_wave[n], out);
+                                jpo = O::fma(Kp, jp, O::mul(Bp, O::sub(out, ez)));
+                            }
+                            if (clampnan && dev_isnan(out)) out = Real(0);
+                            // receivers (owned cells only, so each sample is written once)
+                            if ((mb & kMatRx) && owned[c]) {
+                                for (int rr = 0; rr < D.nrx; ++rr)
+                                    if (D.rx[2 * rr] == x && D.rx[2 * rr + 1] == m)
+                                        D.traces[(size_t)rr * S + n] = out;
+                            }
+                        }
+                        oz[c] = out;
+                        oj[c] = jpo;
+                    }
+                    // running DFT on the NTFF contour
+                    if (nfreq > 0) {
+                        const Real* ph = phasor + (size_t)n * nfreq * 4;
+                        // horizontal faces: face row m-1 is complete at this level
+                        if (m - 1 == fd || m - 1 == ny - fd - 1) {
+                            const bool yp = (m - 1 == ny - fd - 1);
+#pragma unroll
+                            for (int c = 0; c < COLS; ++c) {
+                                const int x = xcol[c];
+                                if (owned[c] && x >= fd + 1 && x <= nx - fd - 2) {
+                                    Real e = O::mul(O::add(ezn[k][c], oz[c]), Real(0.5));
+                                    Real h = hxn[k][c];
+                                    int ci = yp ? contour_index_yp(nx, ny, fd, x) : contour_index_yn(nx, ny, fd, x);
+                                    if (yp) { e = -e; h = -h; }
+                                    dft_update(acc, ph, nfreq, C, ci, h, e);
+                                }
+                            }
+                        }
+                        // vertical faces: buffer (h, e) samples per row for a warp-wide flush
+                        if ((has_face0 || has_face1) && m >= fd && m <= ny - fd - 1) {
+                            Real ezR2_last = __shfl_down_sync(0xffffffffu, oz[0], 1);
+#pragma unroll
+                            for (int c = 0; c < COLS; ++c) {
+                                if (face_slot[c] >= 0) {
+                                    Real ezR2 = (c + 1 < COLS) ? oz[c + 1] : ezR2_last;
+                                    Real e = O::mul(O::add(oz[c], ezR2), Real(0.5));
+                                    Real* s = sm.ring[wib][face_slot[c]][m % kRing][k];
+                                    s[0] = oy[c];
+                                    s[1] = e;
+                                }
+                            }
+                        }
+                    }
+                } else {
+                    // beyond the last time step: pass through unchanged
+#pragma unroll
+                    for (int c = 0; c < COLS; ++c) {
+                        oz[c] = pz[k][c]; ox[c] = px_[k][c]; oy[c] = py_[k][c]; oj[c] = pj[k][c];
+                        const int x = xcol[c];
+                        const int pos = lane * COLS + c;
+                        const bool evalid = pos >= k + 1 && pos <= P - 2 - k;
+                        const bool hvalid = pos >= k && pos <= P - 2 - k;
+                        if (ixh[c] >= 0 && m < ny && hvalid) {
+                            const int xsx = (x < nc) ? x : x - (nx - nc) + nc;
+                            size_t o = psx_h + (size_t)m * 2 * nc + xsx;
+                            psi_copy(k + 1)[o] = psi_copy(k)[o];
+                        }
+                        if (ixe[c] >= 0 && m >= 1 && m <= ny - 1 && evalid) {
+                            const int xsx = (x <= nc) ? x - 1 : x - (nx - nc) + nc;
+                            size_t o = psx_e + (size_t)m * 2 * nc + xsx;
+                            psi_copy(k + 1)[o] = psi_copy(k)[o];
+                        }
+                        if (x >= 0 && x <= nx) {
+                            const int iyh = (m < nc) ? m : ((m >= ny - nc && m < ny) ? m - (ny - nc) + nc : -1);
+                            if (iyh >= 0 && x < nx && hvalid) {
+                                size_t o = psy_h + (size_t)iyh * (nx + 1) + x;
+                                psi_copy(k + 1)[o] = psi_copy(k)[o];
+                            }
+                            const int iye = (m >= 1 && m <= nc) ? m - 1
+                                            : ((m >= ny - nc && m <= ny - 1) ? m - (ny - nc) + nc : -1);
+                            if (iye >= 0 && evalid) {
+                                size_t o = psy_e + (size_t)iye * (nx + 1) + x;
+                                psi_copy(k + 1)[o] = psi_copy(k)[o];
+                            }
+                        }
+                    }
+                }
+                // ---- emit row m
+#pragma unroll
+                for (int c = 0; c < COLS; ++c) {
+                    hxn[k][c] = ox[c];
+                    ezn[k][c] = oz[c];
+                }
+                if (k + 1 < T) {
+                    hmat[k + 1] = pmat[k];
+#pragma unroll
+                    for (int c = 0; c < COLS; ++c) {
+                        hz[k + 1][c] = oz[c]; hxr[k + 1][c] = ox[c]; hyr[k + 1][c] = oy[c]; hj[k + 1][c] = oj[c];
+                    }
+                } else {
+                    const long long rowoff = (long long)m * pitch;
+                    const bool jrow = m >= jy0 && m <= jy1;
+#pragma unroll
+                    for (int c = 0; c < COLS; ++c) {
+                        if (owned[c]) {
+                            const int x = xcol[c];
+                            ez_d[rowoff + x] = oz[c];
+                            hx_d[rowoff + x] = ox[c];
+                            hy_d[rowoff + x] = oy[c];
+                            if (jrow && x >= jx0 && x <= jx1) jp_d[rowoff + x] = oj[c];
+                        }
+                    }
+                }
+            }
+            // the received row becomes this level's previous row
+            pmat[k] = im;
+#pragma unroll
+            for (int c = 0; c < COLS; ++c) {
+                pz[k][c] = iz[c]; px_[k][c] = ix[c]; py_[k][c] = iy[c]; pj[k][c] = ij[c];
+            }
+        }
+
+        // ---- vertical-face DFT flush: rows whose T levels are all done
+        if (has_face0 || has_face1) {
+            const int done = r - 2 * T + 1;   // last row completed by level T-1
+            const bool last = (r == rmax);
+            if (last || ((done + 1 - flushed) >= 32)) {
+                __syncwarp();
+                const int upto = last ? ny : done;
+                while (flushed <= upto) {
+                    const int m = flushed + lane;
+                    if (m <= upto && m >= fd && m <= ny - fd - 1) {
+                        for (int face = 0; face < 2; ++face) {
+                            if (!(face == 0 ? has_face0 : has_face1)) continue;
+                            const int ci = face == 0 ? contour_index_xn(nx, ny, fd, m) : contour_index_xp(nx, ny, fd, m);
+                            const Real sgn = face == 0 ? Real(-1) : Real(1);
+                            for (int f = 0; f < nfreq; ++f) {
+                                Real* a = acc + ((size_t)f * C + ci) * 8;
+                                Real s0 = a[0], s1 = a[1], c0 = a[2], c1 = a[3], s2 = a[4], s3 = a[5], c2 = a[6],
+                                     c3 = a[7];
+                                for (int k = 0; k < nsteps; ++k) {
+                                    const Real* p = phasor + ((size_t)(n0 + k) * nfreq + f) * 4;
+                                    const Real* sm_s = sm.ring[wib][face][m % kRing][k];
+                                    Real h = sgn * sm_s[0], e = sgn * sm_s[1];
+                                    acc_add(s0, c0, Op<Real>::mul(h, p[0]));
+                                    acc_add(s1, c1, Op<Real>::mul(h, p[1]));
+                                    acc_add(s2, c2, Op<Real>::mul(e, p[2]));
+                                    acc_add(s3, c3, Op<Real>::mul(e, p[3]));
+                                }
+                                a[0] = s0; a[1] = s1; a[2] = c0; a[3] = c1;
+                                a[4] = s2; a[5] = s3; a[6] = c2; a[7] = c3;
+                            }
+                        }
+                    }
+                    flushed += 32;
+                }
+                if (flushed > upto + 1) flushed = upto + 1;
+                __syncwarp();
+            }
+        }
+    }
+    cp_async_wait<0>();   // the ring is reused by the warp's next item
+    __syncwarp();
+}
+
+#ifndef TOMO_ADVANCE_MINB
+#define TOMO_ADVANCE_MINB 1   // minimum resident blocks per SM requested from ptxas
+#endif
+
+template <typename Real, int T, int COLS, int MODE>
+__global__ void __launch_bounds__(128, TOMO_ADVANCE_MINB) fdtd_advance_kernel(const SolveDesc<Real>* __restrict__ descs,
+                                                          const WorkItem* __restrict__ items, int nitems) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    AdvanceSmem<Real, T, COLS>& sm = *reinterpret_cast<AdvanceSmem<Real, T, COLS>*>(smem_raw);
+    const int wib = threadIdx.x >> 5;
+    const int warps_per_block = blockDim.x >> 5;
+    const int gw = blockIdx.x * warps_per_block + wib;
+    const int nw = gridDim.x * warps_per_block;
+    for (int it = gw; it < nitems; it += nw) {
+        const WorkItem wi = items[it];
+        const SolveDesc<Real>* __restrict__ D = descs + wi.solve;
+        if (!D->active) continue;
+        advance_item<Real, T, COLS, MODE>(D, wi.strip, sm, wib);
+        __syncwarp();
+    }
+}
+
+}  // namespace tomo
