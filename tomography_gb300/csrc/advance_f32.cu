@@ -7,7 +7,7 @@
 namespace tomo {
 
 template <typename Real>
-using AdvanceFn = void (*)(const SolveDesc<Real>*, const WorkItem*, int);
+using AdvanceFn = void (*)(const SolveDesc<Real>*, const WorkItem*, int, int*);
 
 template <typename Real>
 AdvanceFn<Real> advance_kernel_for(int T, int cols, int mode);
@@ -25,9 +25,7 @@ AdvanceFn<float> advance_kernel_for<float>(int T, int cols, int mode) {
     TOMO_F32_CASE(kModeBreast, 4, 1)
     TOMO_F32_CASE(kModeBreast, 4, 2)
     TOMO_F32_CASE(kModeBreast, 6, 1)
-    TOMO_F32_CASE(kModeBreast, 6, 2)
     TOMO_F32_CASE(kModeBreast, 8, 1)
-    TOMO_F32_CASE(kModeBreast, 8, 2)
     TOMO_F32_CASE(kModeRef, 1, 1)
     TOMO_F32_CASE(kModeRef, 2, 1)
     TOMO_F32_CASE(kModeRef, 4, 1)
@@ -43,9 +41,7 @@ size_t advance_smem_bytes<float>(int T, int cols) {
     if (T == 4 && cols == 1) return sizeof(AdvanceSmem<float, 4, 1>);
     if (T == 4 && cols == 2) return sizeof(AdvanceSmem<float, 4, 2>);
     if (T == 6 && cols == 1) return sizeof(AdvanceSmem<float, 6, 1>);
-    if (T == 6 && cols == 2) return sizeof(AdvanceSmem<float, 6, 2>);
     if (T == 8 && cols == 1) return sizeof(AdvanceSmem<float, 8, 1>);
-    if (T == 8 && cols == 2) return sizeof(AdvanceSmem<float, 8, 2>);
     return 0;
 }
 

@@ -6,7 +6,7 @@
 namespace tomo {
 
 template <typename Real>
-using AdvanceFn = void (*)(const SolveDesc<Real>*, const WorkItem*, int);
+using AdvanceFn = void (*)(const SolveDesc<Real>*, const WorkItem*, int, int*);
 
 template <typename Real>
 AdvanceFn<Real> advance_kernel_for(int T, int cols, int mode);

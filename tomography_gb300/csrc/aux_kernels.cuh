@@ -75,8 +75,9 @@ __global__ void material_table_kernel(const double* __restrict__ mp, Real* __res
 
 // Progress every active solve by T steps after an advance launch.
 template <typename Real>
-__global__ void bump_kernel(SolveDesc<Real>* descs, int nsolves, int T) {
+__global__ void bump_kernel(SolveDesc<Real>* descs, int nsolves, int T, int* counter) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s == 0) *counter = 0;   // work counter of the next advance launch
     if (s >= nsolves) return;
     SolveDesc<Real>& D = descs[s];
     if (D.active && D.step < D.steps_total) {

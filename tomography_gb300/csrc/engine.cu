@@ -431,6 +431,8 @@ int EngineT<Real>::init(const ProblemClass& pc) {
     CUDA_TRY(cudaGetDevice(&dev));
     CUDA_TRY(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, dev));
     TOMO_TRY(cd_.init(pc));
+    TOMO_TRY(d_counter_.ensure(sizeof(int) * 4));
+    CUDA_TRY(cudaMemset(d_counter_.p, 0, sizeof(int) * 4));
     // tuning: explicit spec values, else environment, else defaults
     T_ = pc.spec.steps_per_launch;
     cols_ = pc.spec.cols_per_lane;
@@ -521,7 +523,7 @@ int EngineT<Real>::build_graph(int nlaunch) {
     CUDA_TRY(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
     for (int l = 0; l < nlaunch; ++l)
         launch_advance<Real>(T_, cols_, advance_mode(cd_.pc.spec), blocks, smem, d_descs_.as<SolveDesc<Real>>(),
-                             d_items_.as<WorkItem>(), nitems_, nsolves_, stream_);
+                             d_items_.as<WorkItem>(), nitems_, nsolves_, d_counter_.as<int>(), stream_);
     cudaError_t ce = cudaStreamEndCapture(stream_, &graph);
     if (ce != cudaSuccess) return fail(TOMO_ECUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
     ce = cudaGraphInstantiate(&graph_exec_, graph, 0);
@@ -573,7 +575,7 @@ int EngineT<Real>::forward(const double* args, size_t ncand, size_t nparam, cons
         for (int sv = 0; sv < nsolves; ++sv)
             for (int l = 0; l < nlaunch; ++l)
                 launch_advance<Real>(T_, cols_, advance_mode(s), blocks, smem, d_descs_.as<SolveDesc<Real>>() + sv,
-                                     d_items_.as<WorkItem>(), per, 1, stream_);
+                                     d_items_.as<WorkItem>(), per, 1, d_counter_.as<int>(), stream_);
         CUDA_TRY(cudaEventRecord(ev_[2], stream_));
         kernels += 2 * (int64_t)nlaunch * nsolves;
     } else {

@@ -98,7 +98,7 @@ struct Unpacked {
 int unpack_args(const ProblemClass& pc, const double* args, size_t ncand, size_t nparam, Unpacked& u);
 
 template <typename Real>
-using AdvanceFn = void (*)(const SolveDesc<Real>*, const WorkItem*, int);
+using AdvanceFn = void (*)(const SolveDesc<Real>*, const WorkItem*, int, int*);
 template <typename Real>
 AdvanceFn<Real> advance_kernel_for(int T, int cols, int mode);
 
@@ -309,18 +309,24 @@ int advance_grid(int T, int cols, int mode, int nitems, int num_sms, int* blocks
 
 template <typename Real>
 void launch_advance(int T, int cols, int mode, int blocks, size_t smem, const SolveDesc<Real>* descs,
-                    const WorkItem* items, int nitems, int nsolves, cudaStream_t st) {
+                    const WorkItem* items, int nitems, int nsolves, int* counter, cudaStream_t st) {
     AdvanceFn<Real> fn = advance_kernel_for<Real>(T, cols, mode);
-    fn<<<blocks, 128, smem, st>>>(descs, items, nitems);
-    bump_kernel<Real><<<(nsolves + 127) / 128, 128, 0, st>>>(const_cast<SolveDesc<Real>*>(descs), nsolves, T);
+    fn<<<blocks, 128, smem, st>>>(descs, items, nitems, counter);
+    bump_kernel<Real><<<(nsolves + 127) / 128, 128, 0, st>>>(const_cast<SolveDesc<Real>*>(descs), nsolves, T, counter);
 }
 
-// Work items (solve, strip) for nsolves solves starting at solve index first.
+// Work items (solve, strip) for nsolves solves starting at solve index first:
+// the edge strips (CPML, PEC boundary, vertical NTFF faces: the expensive
+// ones) of every solve first, then the interior strips.
 inline void append_items(std::vector<WorkItem>& items, int first, int nsolves, int nx, int T, int cols) {
     const int W = 32 * cols - 2 * T;
     const int nstrips = (nx + 1 + W - 1) / W;
+    for (int sv = 0; sv < nsolves; ++sv) {
+        items.push_back({first + sv, 0});
+        if (nstrips > 1) items.push_back({first + sv, nstrips - 1});
+    }
     for (int sv = 0; sv < nsolves; ++sv)
-        for (int q = 0; q < nstrips; ++q) items.push_back({first + sv, q});
+        for (int q = 1; q + 1 < nstrips; ++q) items.push_back({first + sv, q});
 }
 
 // ------------------------------------------------------------------- engine
@@ -371,7 +377,7 @@ class EngineT : public EngineBase {
     // batch buffers
     int cap_cand_ = 0, cur_cand_ = 0, nsolves_ = 0, nitems_ = 0;
     DevBuf d_state_, d_mats_, d_tabs_, d_upload_, d_descs_, d_items_, d_partials_, d_fit_, d_D_, d_P_, d_flag_, d_trf_,
-        d_trd_;
+        d_trd_, d_counter_;
     Unpacked up_;
     std::vector<SolveDesc<Real>> h_descs_;
     cudaGraphExec_t graph_exec_ = nullptr;

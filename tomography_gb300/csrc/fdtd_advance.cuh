@@ -139,10 +139,22 @@ __device__ __forceinline__ void dft_update(Real* acc, const Real* ph, int nfreq,
     }
 }
 
+// Ca, Cb, Cj, Bp of one material from the per-warp table (one 16-byte load in FP32).
+__device__ __forceinline__ void load_coefs(const float* t, float& a, float& b, float& c, float& d) {
+    const float4 v = *reinterpret_cast<const float4*>(t);
+    a = v.x; b = v.y; c = v.z; d = v.w;
+}
+__device__ __forceinline__ void load_coefs(const double* t, double& a, double& b, double& c, double& d) {
+    const double2 v0 = reinterpret_cast<const double2*>(t)[0], v1 = reinterpret_cast<const double2*>(t)[1];
+    a = v0.x; b = v0.y; c = v1.x; d = v1.y;
+}
+
 // Dynamic shared memory per block (4 warps).
 template <typename Real, int T, int COLS>
 struct AdvanceSmem {
     Real rows[4][kRowSlots][4][32 * COLS];   // per-warp prefetch ring: Ez, Hx, Hy, Jp of kRowSlots rows
+    Real psring[4][kRowSlots][4][32 * COLS]; // per-warp prefetch ring: CPML psi (hyx, ezx, hxy, ezy) at time n0
+    Real pslev[4][T > 1 ? T - 1 : 1][4][4][32 * COLS];   // psi after level k, 4 rows in flight
     Real tab[4][kMaxMat][4];                 // per-warp Ca, Cb, Cj, Bp of every material
     Real ring[4][2][kRing][T][2];            // per-warp vertical-face DFT samples (h, e)
     uint32_t rowbits[4][kMaxRowWords];       // per-warp "row needs the general path" flags
@@ -263,12 +275,24 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, 
     Real* __restrict__ hx_d = D.hx[dst];
     Real* __restrict__ hy_d = D.hy[dst];
     Real* __restrict__ jp_d = D.jp[dst];
-    auto psi_copy = [&](int level) -> Real* {
-        // time copy holding psi at time n0+level
-        if (level == 0) return D.psi[src];
-        if (level == T) return D.psi[dst];
-        return D.psi_scratch + (size_t)(level - 1) * D.psi_stride;
+    // CPML psi, fields 0 hyx, 1 ezx (x strips), 2 hxy, 3 ezy (y strips).  Time
+    // n0 comes from the global copy of the previous launch (prefetched with the
+    // row), intermediate time levels live in warp-private shared memory, and
+    // the last level writes the owned columns of the next global copy.
+    const Real* __restrict__ psi_src = D.psi[src];
+    Real* __restrict__ psi_dst = D.psi[dst];
+    auto psi_in = [&](int k, int f, int m, int c) -> Real {
+        if (k == 0) return sm.psring[wib][m & (kRowSlots - 1)][f][lane * COLS + c];
+        return sm.pslev[wib][(k - 1) % (T > 1 ? T - 1 : 1)][f][m & 3][lane * COLS + c];
     };
+    auto psi_out = [&](int k, int f, int m, int c, Real v, size_t goff) {
+        if (k + 1 < T) sm.pslev[wib][k % (T > 1 ? T - 1 : 1)][f][m & 3][lane * COLS + c] = v;
+        else if (owned[c]) psi_dst[goff] = v;
+    };
+    bool wxs = false;   // warp holds an x-strip column (uniform)
+#pragma unroll
+    for (int c = 0; c < COLS; ++c) wxs |= ixh[c] >= 0 || ixe[c] >= 0;
+    wxs = __any_sync(0xffffffffu, wxs);
 
     // Rows stream through a per-warp shared-memory ring: row r + kPrefetch is
     // requested (cp.async) while row r is consumed, so kPrefetch rows of every
@@ -291,6 +315,34 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, 
         if (lane <= P / 4)
             cp_async<4>(&sm.mats[wib][slot][4 * lane], matp + (long long)(valid ? r : 0) * mpitch + mstart + 4 * lane,
                         valid);
+        if (wxs) {
+#pragma unroll
+            for (int c = 0; c < COLS; ++c) {
+                const int x = xcol[c];
+                const bool hv = valid && ixh[c] >= 0 && r < ny;
+                const bool ev = valid && ixe[c] >= 0 && r >= 1 && r <= ny - 1;
+                const int xh = (x < nc) ? x : x - (nx - nc) + nc;
+                const int xe = (x <= nc) ? x - 1 : x - (nx - nc) + nc;
+                cp_async<sizeof(Real)>(&sm.psring[wib][slot][0][lane * COLS + c],
+                                       psi_src + (hv ? psx_h + (size_t)r * 2 * nc + xh : 0), hv);
+                cp_async<sizeof(Real)>(&sm.psring[wib][slot][1][lane * COLS + c],
+                                       psi_src + (ev ? psx_e + (size_t)r * 2 * nc + xe : 0), ev);
+            }
+        }
+        if (valid && (r <= nc || r >= ny - nc)) {
+            const int yh = (r < nc) ? r : ((r >= ny - nc && r < ny) ? r - (ny - nc) + nc : -1);
+            const int ye = (r >= 1 && r <= nc) ? r - 1 : ((r >= ny - nc && r <= ny - 1) ? r - (ny - nc) + nc : -1);
+#pragma unroll
+            for (int c = 0; c < COLS; ++c) {
+                const int x = xcol[c];
+                const bool hv = yh >= 0 && x >= 0 && x < nx;
+                const bool ev = ye >= 0 && x >= 1 && x <= nx - 1;
+                cp_async<sizeof(Real)>(&sm.psring[wib][slot][2][lane * COLS + c],
+                                       psi_src + (hv ? psy_h + (size_t)yh * (nx + 1) + x : 0), hv);
+                cp_async<sizeof(Real)>(&sm.psring[wib][slot][3][lane * COLS + c],
+                                       psi_src + (ev ? psy_e + (size_t)ye * (nx + 1) + x : 0), ev);
+            }
+        }
         cp_async_commit();
     };
 #pragma unroll 1
@@ -316,7 +368,6 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, 
                 lm |= (uint32_t)sm.mats[wib][slot][moff + lane * COLS + c] << (8 * c);
             }
         }
-        issue_row(r + kPrefetch);
 
 #pragma unroll
         for (int k = T - 1; k >= 0; --k) {
@@ -333,7 +384,8 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, 
             if (m >= 0) {
                 Real oz[COLS], ox[COLS], oy[COLS], oj[COLS];
                 const int n = n0 + k;        // time step index computed by this level
-                const bool fast = !wspecial && !((rowbits[m >> 5] >> (m & 31)) & 1u);
+                const bool rowbit = (rowbits[m >> 5] >> (m & 31)) & 1u;
+                const bool fast = !wspecial && !rowbit;
                 if (k < nsteps && fast) {
                     // ================= fast path: interior Yee + Debye
                     const Real ezR_last = __shfl_down_sync(0xffffffffu, pz[k][0], 1);
@@ -352,8 +404,8 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, 
 #pragma unroll
                     for (int c = 0; c < COLS; ++c) {
                         const int mi = (pmat[k] >> (8 * c)) & kMatMask;
-                        const Real Ca = sm.tab[wib][mi][kCa], Cb = sm.tab[wib][mi][kCb];
-                        const Real Cj = sm.tab[wib][mi][kCj], Bp = sm.tab[wib][mi][kBp];
+                        Real Ca, Cb, Cj, Bp;
+                        load_coefs(sm.tab[wib][mi], Ca, Cb, Cj, Bp);
                         const Real hyL = (c > 0) ? oy[c - 1] : hyL_first;
                         const Real dHy = O::sub(oy[c], hyL);
                         const Real dHx = O::sub(ox[c], hxn[k][c]);
@@ -378,8 +430,6 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, 
                         Real ezR = (c + 1 < COLS) ? pz[k][c + 1] : ezR_last;
                         Real hx0 = px_[k][c], hy0 = py_[k][c];
                         Real hx = hx0, hy = hy0;
-                        const int pos = lane * COLS + c;
-                        const bool hvalid = pos >= k && pos <= P - 2 - k;
                         if (hrow && x >= 0 && x < nx) {
                             Real dEy = O::sub(ezR, ez0);
                             Real dEx = O::sub(iz[c], ez0);
@@ -388,19 +438,15 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, 
                             if (ixh[c] >= 0) {
                                 const int i = ixh[c];
                                 const int xsx = (x < nc) ? x : x - (nx - nc) + nc;
-                                Real* pin = psi_copy(k) + psx_h + (size_t)m * 2 * nc + xsx;
-                                Real* pout = psi_copy(k + 1) + psx_h + (size_t)m * 2 * nc + xsx;
-                                Real ps = O::fma(cpml[4 * nc + i], *pin, O::mul(cpml[5 * nc + i], dEy));
-                                if (hvalid) *pout = ps;
+                                Real ps = O::fma(cpml[4 * nc + i], psi_in(k, 0, m, c), O::mul(cpml[5 * nc + i], dEy));
+                                psi_out(k, 0, m, c, ps, psx_h + (size_t)m * 2 * nc + xsx);
                                 hy = O::fma(O::mul(chez, dEy), cpml[3 * nc + i], hy0);
                                 hy = O::fma(O::mul(chez, dxr), ps, hy);
                             }
                             if (iyh >= 0) {
                                 const int ysx = (m < nc) ? m : m - (ny - nc) + nc;
-                                Real* pin = psi_copy(k) + psy_h + (size_t)ysx * (nx + 1) + x;
-                                Real* pout = psi_copy(k + 1) + psy_h + (size_t)ysx * (nx + 1) + x;
-                                Real ps = O::fma(cpml[4 * nc + iyh], *pin, O::mul(cpml[5 * nc + iyh], dEx));
-                                if (hvalid) *pout = ps;
+                                Real ps = O::fma(cpml[4 * nc + iyh], psi_in(k, 2, m, c), O::mul(cpml[5 * nc + iyh], dEx));
+                                psi_out(k, 2, m, c, ps, psy_h + (size_t)ysx * (nx + 1) + x);
                                 hx = O::fma(-O::mul(chez, dEx), cpml[3 * nc + iyh], hx0);
                                 hx = O::fma(-O::mul(chez, dxr), ps, hx);
                             }
@@ -418,8 +464,6 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, 
 #pragma unroll
                     for (int c = 0; c < COLS; ++c) {
                         const int x = xcol[c];
-                        const int pos = lane * COLS + c;
-                        const bool evalid = pos >= k + 1 && pos <= P - 2 - k;
                         Real ez = pz[k][c];
                         Real jp = pj[k][c];
                         Real out = Real(0);
@@ -456,20 +500,16 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, 
                                 if (ixe[c] >= 0) {
                                     const int i = ixe[c];
                                     const int xsx = (x <= nc) ? x - 1 : x - (nx - nc) + nc;
-                                    Real* pin = psi_copy(k) + psx_e + (size_t)m * 2 * nc + xsx;
-                                    Real* pout = psi_copy(k + 1) + psx_e + (size_t)m * 2 * nc + xsx;
-                                    Real ps = O::fma(cpml[nc + i], *pin, O::mul(cpml[2 * nc + i], dHy));
-                                    if (evalid) *pout = ps;
+                                    Real ps = O::fma(cpml[nc + i], psi_in(k, 1, m, c), O::mul(cpml[2 * nc + i], dHy));
+                                    psi_out(k, 1, m, c, ps, psx_e + (size_t)m * 2 * nc + xsx);
                                     const Real rk = cpml[i];
                                     out = O::fma(Ca, ez, O::mul(O::mul(Cb, O::sub(dHy, dHx)), rk));
                                     out = O::fma(O::mul(Cb, dxr), ps, out);
                                 }
                                 if (iye >= 0) {
                                     const int ysx = (m <= nc) ? m - 1 : m - (ny - nc) + nc;
-                                    Real* pin = psi_copy(k) + psy_e + (size_t)ysx * (nx + 1) + x;
-                                    Real* pout = psi_copy(k + 1) + psy_e + (size_t)ysx * (nx + 1) + x;
-                                    Real ps = O::fma(cpml[nc + iye], *pin, O::mul(cpml[2 * nc + iye], dHx));
-                                    if (evalid) *pout = ps;
+                                    Real ps = O::fma(cpml[nc + iye], psi_in(k, 3, m, c), O::mul(cpml[2 * nc + iye], dHx));
+                                    psi_out(k, 3, m, c, ps, psy_e + (size_t)ysx * (nx + 1) + x);
                                     const Real rk = cpml[iye];
                                     out = O::fma(Ca, ez, O::mul(O::mul(Cb, O::sub(dHy, dHx)), rk));
                                     out = O::fma(-O::mul(Cb, dxr), ps, out);
@@ -479,18 +519,14 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, 
                                 if (ixe[c] >= 0) {
                                     const int i = ixe[c];
                                     const int xsx = (x <= nc) ? x - 1 : x - (nx - nc) + nc;
-                                    Real* pin = psi_copy(k) + psx_e + (size_t)m * 2 * nc + xsx;
-                                    Real* pout = psi_copy(k + 1) + psx_e + (size_t)m * 2 * nc + xsx;
-                                    qx = O::fma(cpml[nc + i], *pin, O::mul(cpml[2 * nc + i], dHy));
-                                    if (evalid) *pout = qx;
+                                    qx = O::fma(cpml[nc + i], psi_in(k, 1, m, c), O::mul(cpml[2 * nc + i], dHy));
+                                    psi_out(k, 1, m, c, qx, psx_e + (size_t)m * 2 * nc + xsx);
                                     cx = O::mul(dHy, cpml[i]);
                                 }
                                 if (iye >= 0) {
                                     const int ysx = (m <= nc) ? m - 1 : m - (ny - nc) + nc;
-                                    Real* pin = psi_copy(k) + psy_e + (size_t)ysx * (nx + 1) + x;
-                                    Real* pout = psi_copy(k + 1) + psy_e + (size_t)ysx * (nx + 1) + x;
-                                    qy = O::fma(cpml[nc + iye], *pin, O::mul(cpml[2 * nc + iye], dHx));
-                                    if (evalid) *pout = qy;
+                                    qy = O::fma(cpml[nc + iye], psi_in(k, 3, m, c), O::mul(cpml[2 * nc + iye], dHx));
+                                    psi_out(k, 3, m, c, qy, psy_e + (size_t)ysx * (nx + 1) + x);
                                     cy = O::mul(dHx, cpml[iye]);
                                 }
                                 // proper CPML: both stretched derivatives and both psi terms
@@ -547,36 +583,27 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, 
                         }
                     }
                 } else {
-                    // beyond the last time step: pass through unchanged
+                    // beyond the last time step: pass through unchanged (psi included)
 #pragma unroll
                     for (int c = 0; c < COLS; ++c) {
                         oz[c] = pz[k][c]; ox[c] = px_[k][c]; oy[c] = py_[k][c]; oj[c] = pj[k][c];
                         const int x = xcol[c];
-                        const int pos = lane * COLS + c;
-                        const bool evalid = pos >= k + 1 && pos <= P - 2 - k;
-                        const bool hvalid = pos >= k && pos <= P - 2 - k;
-                        if (ixh[c] >= 0 && m < ny && hvalid) {
+                        if (ixh[c] >= 0 && m < ny) {
                             const int xsx = (x < nc) ? x : x - (nx - nc) + nc;
-                            size_t o = psx_h + (size_t)m * 2 * nc + xsx;
-                            psi_copy(k + 1)[o] = psi_copy(k)[o];
+                            psi_out(k, 0, m, c, psi_in(k, 0, m, c), psx_h + (size_t)m * 2 * nc + xsx);
                         }
-                        if (ixe[c] >= 0 && m >= 1 && m <= ny - 1 && evalid) {
+                        if (ixe[c] >= 0 && m >= 1 && m <= ny - 1) {
                             const int xsx = (x <= nc) ? x - 1 : x - (nx - nc) + nc;
-                            size_t o = psx_e + (size_t)m * 2 * nc + xsx;
-                            psi_copy(k + 1)[o] = psi_copy(k)[o];
+                            psi_out(k, 1, m, c, psi_in(k, 1, m, c), psx_e + (size_t)m * 2 * nc + xsx);
                         }
                         if (x >= 0 && x <= nx) {
                             const int iyh = (m < nc) ? m : ((m >= ny - nc && m < ny) ? m - (ny - nc) + nc : -1);
-                            if (iyh >= 0 && x < nx && hvalid) {
-                                size_t o = psy_h + (size_t)iyh * (nx + 1) + x;
-                                psi_copy(k + 1)[o] = psi_copy(k)[o];
-                            }
+                            if (iyh >= 0 && x < nx)
+                                psi_out(k, 2, m, c, psi_in(k, 2, m, c), psy_h + (size_t)iyh * (nx + 1) + x);
                             const int iye = (m >= 1 && m <= nc) ? m - 1
                                             : ((m >= ny - nc && m <= ny - 1) ? m - (ny - nc) + nc : -1);
-                            if (iye >= 0 && evalid) {
-                                size_t o = psy_e + (size_t)iye * (nx + 1) + x;
-                                psi_copy(k + 1)[o] = psi_copy(k)[o];
-                            }
+                            if (iye >= 0 && x >= 1 && x <= nx - 1)
+                                psi_out(k, 3, m, c, psi_in(k, 3, m, c), psy_e + (size_t)iye * (nx + 1) + x);
                         }
                     }
                 }
@@ -653,6 +680,9 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, 
                 __syncwarp();
             }
         }
+        // request row r + kPrefetch into the slot of row r - 1 (no longer read)
+        __syncwarp();
+        issue_row(r + kPrefetch);
     }
     cp_async_wait<0>();   // the ring is reused by the warp's next item
     __syncwarp();
@@ -662,16 +692,21 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, 
 #define TOMO_ADVANCE_MINB 1   // minimum resident blocks per SM requested from ptxas
 #endif
 
+// Persistent kernel: warps take work items from a global counter (reset by the
+// progress kernel after every launch), most expensive items first.
 template <typename Real, int T, int COLS, int MODE>
 __global__ void __launch_bounds__(128, TOMO_ADVANCE_MINB) fdtd_advance_kernel(const SolveDesc<Real>* __restrict__ descs,
-                                                          const WorkItem* __restrict__ items, int nitems) {
+                                                          const WorkItem* __restrict__ items, int nitems,
+                                                          int* __restrict__ counter) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     AdvanceSmem<Real, T, COLS>& sm = *reinterpret_cast<AdvanceSmem<Real, T, COLS>*>(smem_raw);
     const int wib = threadIdx.x >> 5;
-    const int warps_per_block = blockDim.x >> 5;
-    const int gw = blockIdx.x * warps_per_block + wib;
-    const int nw = gridDim.x * warps_per_block;
-    for (int it = gw; it < nitems; it += nw) {
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int it = 0;
+        if (lane == 0) it = atomicAdd(counter, 1);
+        it = __shfl_sync(0xffffffffu, it, 0);
+        if (it >= nitems) break;
         const WorkItem wi = items[it];
         const SolveDesc<Real>* __restrict__ D = descs + wi.solve;
         if (!D->active) continue;

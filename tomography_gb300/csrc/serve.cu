@@ -310,8 +310,8 @@ int EngineT<Real>::serve_step(int* n_active) {
     int running = 0;
     if (st->nitems > 0) {
         launch_advance<Real>(T_, cols_, advance_mode(cd_.pc.spec), st->blocks, st->smem,
-                             st->descs.template as<SolveDesc<Real>>(),
-                             st->items.template as<WorkItem>(), st->nitems, st->hi_slot, stream_);
+                             st->descs.template as<SolveDesc<Real>>(), st->items.template as<WorkItem>(), st->nitems,
+                             st->hi_slot, d_counter_.as<int>(), stream_);
         CUDA_TRY(cudaGetLastError());
         for (auto& kv : st->reqs) {
             ServeRequest<Real>& r = *kv.second;
