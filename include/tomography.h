@@ -160,6 +160,22 @@ int tomo_serve_step(tomo_handle *h, int *n_active);
 int tomo_poll(tomo_handle *h, uint64_t ticket, double *fitness);
 int tomo_cancel(tomo_handle *h, uint64_t ticket);
 
+/* ---- trace misfit without allocation.  No counterpart in the reference.
+   For callers that cannot call cudaMalloc: a host framework whose caching
+   allocator owns the device memory, or a latency-critical serving loop that
+   must not take the device synchronisation of cudaMalloc/cudaFree.  Computes
+   fitness[c] = -sum (s - t)^2 / sum t^2 of n_cand candidates from device
+   buffers the caller owns -- traces [n_cand][n_tx][n_per_solve] and target
+   [n_tx][n_per_solve] (float), fitness [n_cand] (double) -- asynchronously on
+   `stream` (cudaStream_t as void*, NULL = default stream).  The scratch is a
+   fixed device array of the library: at most 65536 solves (n_cand * n_tx)
+   per call, about 1 MiB that every GPU loading the library holds until exit;
+   larger problems return TOMO_EINVAL.  The first call on a device looks the
+   array up, so make it before any stream capture.  All calls share the array:
+   calls whose kernels overlap on the GPU race and must not be issued. */
+int tomo_trace_misfit_static(const float *traces, const float *target, size_t n_cand, size_t n_tx,
+                             size_t n_per_solve, double *fitness, void *stream);
+
 int tomo_get_stats(tomo_handle *h, tomo_stats *stats);
 const char *tomo_last_error(void);
 const char *tomo_version(void);

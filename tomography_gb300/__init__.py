@@ -103,6 +103,7 @@ def library() -> C.CDLL:
         "tomo_poll": (I, [P, C.c_uint64, dp]),
         "tomo_cancel": (I, [P, C.c_uint64]),
         "tomo_get_stats": (I, [P, C.POINTER(Stats)]),
+        "tomo_trace_misfit_static": (I, [C.c_void_p, C.c_void_p, SZ, SZ, SZ, C.c_void_p, C.c_void_p]),
         "tomo_last_error": (C.c_char_p, []),
         "tomo_version": (C.c_char_p, []),
         "tomo_fdtd_gpu_set_target": (I, [fp, SZ]),

@@ -26,6 +26,7 @@ SOURCES = [
     "serve.cu",
     "capi.cpp",
     "fdtd_gpu_dropin.cpp",
+    "noalloc.cu",
 ]
 HEADERS = ["solve_desc.h", "fdtd_advance.cuh", "aux_kernels.cuh", "engine.h", "engine_impl.cuh"]
 
