@@ -83,8 +83,8 @@ typedef struct tomo_spec {
     int32_t ff_norm;           /* 1: reference normalisation (Prad, 33.329), 0: plain */
     int32_t misfit;            /* 0: -sum (D-m)^2/(E F); 1: relative; 2: trace L2    */
     /* engine tuning: 0 = autotune */
-    int32_t steps_per_launch;  /* temporal-blocking depth T                          */
-    int32_t cols_per_lane;     /* columns per lane                                   */
+    int32_t steps_per_launch;  /* temporal-blocking depth T; 0: autotuned            */
+    int32_t cols_per_lane;     /* columns per lane; 0: autotuned                     */
     int32_t plain;             /* 1: one solve per launch sequence, one launch per
                                   step, no CUDA graph (the plain baseline path)      */
 } tomo_spec;
@@ -109,6 +109,11 @@ typedef struct tomo_stats {
     int32_t steps_per_launch; /* T used                                                      */
     int32_t cols_per_lane;    /* COLS used                                                   */
     int64_t h2d_bytes, d2h_bytes;  /* host<->device bytes of the last batch                  */
+    double tune_ms;           /* device time the autotuner spent in the last call (0 when
+                                 the (T, COLS) choice for this batch size was cached)     */
+    int32_t tuned_configs;    /* blockings the autotuner timed in the last call            */
+    int32_t min_blocks_per_sm;/* register budget of the advance kernel used (2: 255 regs,
+                                 3: 168, 4: 128 per thread)                               */
 } tomo_stats;
 
 /* ---- presets */
@@ -118,6 +123,12 @@ int tomo_spec_reference(tomo_spec *spec, int cpu_variant);
 /* Breast-imaging workloads 0..4 (plain forward solve, batched PSO, precision
    study, serving, large batch). */
 int tomo_spec_breast(tomo_spec *spec, int config);
+/* One request of the serving workload: the breast phantom (35 mm disc) at 70%
+   of a 100 mm square domain of edge x edge cells (dx = 0.1 m / edge), steps =
+   4 * edge, n_antennas antennas on the 42 mm ring, every antenna transmitting.
+   No counterpart in the reference (its problem size is compiled in,
+   FDTD_common.hxx:1-76). */
+int tomo_spec_serving(tomo_spec *spec, int edge, int n_antennas);
 /* number of candidate parameters the spec expects (27, 162 or 8*n_ellipses) */
 int tomo_num_params(const tomo_spec *spec);
 /* number of excitations (solves) per candidate */

@@ -53,6 +53,14 @@ def test_presets(tomo):
     assert lib.tomo_num_excitations(C.byref(b)) == 16
     assert lib.tomo_spec_breast(C.byref(b), 9) == -1
     assert b"0..4" in lib.tomo_last_error()
+    # serving requests: the disc stays at 70% of a 100 mm domain, steps = 4 x edge
+    for edge, ant in ((128, 8), (1024, 32)):
+        v = tomo.serving_spec(edge, ant)
+        assert (v.nx, v.ny, v.steps, v.n_antennas, v.n_tx) == (edge, edge, 4 * edge, ant, ant)
+        assert v.dx == pytest.approx(0.1 / edge) and 2 * v.disc_radius / (v.nx * v.dx) == pytest.approx(0.7)
+        assert v.dt == pytest.approx(0.99 * v.dx / (299792458.0 * np.sqrt(2)), rel=1e-4)
+        assert v.cpml_sigma_max == pytest.approx(0.8 * 4 / (376.730313 * v.dx), rel=1e-6)
+    assert lib.tomo_spec_serving(C.byref(b), 32, 8) == -1
 
 
 def test_invalid_specs_are_rejected_before_device_use(tomo):

@@ -64,6 +64,9 @@ class Stats(C.Structure):
         ("cols_per_lane", C.c_int32),
         ("h2d_bytes", C.c_int64),
         ("d2h_bytes", C.c_int64),
+        ("tune_ms", C.c_double),
+        ("tuned_configs", C.c_int32),
+        ("min_blocks_per_sm", C.c_int32),
     ]
 
     def as_dict(self) -> dict:
@@ -86,6 +89,7 @@ def library() -> C.CDLL:
     sig = {
         "tomo_spec_reference": (I, [C.POINTER(Spec), I]),
         "tomo_spec_breast": (I, [C.POINTER(Spec), I]),
+        "tomo_spec_serving": (I, [C.POINTER(Spec), I, I]),
         "tomo_num_params": (I, [C.POINTER(Spec)]),
         "tomo_num_excitations": (I, [C.POINTER(Spec)]),
         "tomo_create": (I, [C.POINTER(Spec), C.POINTER(P)]),
@@ -141,6 +145,14 @@ def breast_spec(config: int) -> Spec:
     """Breast-imaging workload presets 0..4."""
     s = Spec()
     _check(library().tomo_spec_breast(C.byref(s), int(config)))
+    return s
+
+
+def serving_spec(edge: int, n_antennas: int) -> Spec:
+    """One request of the serving workload: edge x edge cells over a 100 mm
+    domain (breast at 70%), 4*edge steps, every antenna transmitting."""
+    s = Spec()
+    _check(library().tomo_spec_serving(C.byref(s), int(edge), int(n_antennas)))
     return s
 
 

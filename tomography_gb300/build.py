@@ -20,15 +20,20 @@ LIB = os.path.join(OUT_DIR, "libtomography_gb300.so")
 REPO = os.path.dirname(HERE)
 
 SOURCES = [
-    "advance_f32.cu",
+    "advance_f32_b1.cu",
+    "advance_f32_b2.cu",
+    "advance_f32_ref.cu",
     "advance_f64.cu",
+    "advance_registry.cu",
     "engine.cu",
     "serve.cu",
     "capi.cpp",
     "fdtd_gpu_dropin.cpp",
     "noalloc.cu",
+    "plain.cu",
 ]
-HEADERS = ["solve_desc.h", "fdtd_advance.cuh", "aux_kernels.cuh", "engine.h", "engine_impl.cuh"]
+HEADERS = ["solve_desc.h", "fdtd_advance.cuh", "aux_kernels.cuh", "engine.h", "engine_impl.cuh", "plain_kernels.cuh",
+           "advance_inst.cuh"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",

@@ -17,6 +17,7 @@ extern "C" {
 
 int tomo_spec_reference(tomo_spec* spec, int cpu_variant) { return tomo::spec_reference(spec, cpu_variant); }
 int tomo_spec_breast(tomo_spec* spec, int config) { return tomo::spec_breast(spec, config); }
+int tomo_spec_serving(tomo_spec* spec, int edge, int n_antennas) { return tomo::spec_serving(spec, edge, n_antennas); }
 int tomo_num_params(const tomo_spec* spec) { return tomo::num_params(spec); }
 int tomo_num_excitations(const tomo_spec* spec) { return tomo::num_excitations(spec); }
 

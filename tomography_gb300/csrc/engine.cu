@@ -77,6 +77,8 @@ int spec_reference(tomo_spec* s, int cpu_variant) {
     return TOMO_OK;
 }
 
+static void breast_derived(tomo_spec* s);
+
 int spec_breast(tomo_spec* s, int config) {
     if (!s) return fail(TOMO_EINVAL, "spec is NULL");
     if (config < 0 || config > 4) return fail(TOMO_EINVAL, "breast config must be 0..4");
@@ -122,6 +124,27 @@ int spec_breast(tomo_spec* s, int config) {
             s->n_angles = 720;
             break;
     }
+    breast_derived(s);
+    return TOMO_OK;
+}
+
+int spec_serving(tomo_spec* s, int edge, int n_antennas) {
+    if (!s) return fail(TOMO_EINVAL, "spec is NULL");
+    if (edge < 64 || edge > 8190) return fail(TOMO_EINVAL, "serving grid edge must be 64..8190");
+    if (n_antennas < 1 || n_antennas > kMaxRx) return fail(TOMO_EINVAL, "n_antennas out of range");
+    TOMO_TRY(spec_breast(s, 3));
+    // the 35 mm disc stays at 70% of a 100 mm square domain whatever the edge
+    s->nx = s->ny = edge;
+    s->dx = 0.1 / edge;
+    s->steps = 4 * edge;
+    s->n_antennas = n_antennas;
+    s->n_tx = n_antennas;
+    breast_derived(s);
+    return TOMO_OK;
+}
+
+// Parameters of the breast-imaging presets that follow from dx.
+static void breast_derived(tomo_spec* s) {
     s->dt = 0.99 * s->dx / (kC0 * std::sqrt(2.0));
     s->cpml_grading = 3;
     s->cpml_sigma_max = 0.8 * (3 + 1) / (kEta0 * s->dx);
@@ -139,7 +162,6 @@ int spec_breast(tomo_spec* s, int config) {
     s->nf2ff_d = s->ncpml + 3;
     s->ff_norm = 0;
     s->misfit = 2;
-    return TOMO_OK;
 }
 
 int num_params(const tomo_spec* s) {
@@ -433,19 +455,95 @@ int EngineT<Real>::init(const ProblemClass& pc) {
     TOMO_TRY(cd_.init(pc));
     TOMO_TRY(d_counter_.ensure(sizeof(int) * 4));
     CUDA_TRY(cudaMemset(d_counter_.p, 0, sizeof(int) * 4));
-    // tuning: explicit spec values, else environment, else defaults
-    T_ = pc.spec.steps_per_launch;
-    cols_ = pc.spec.cols_per_lane;
-    if (T_ <= 0) {
-        const char* e = std::getenv("TOMO_T");
-        T_ = e ? std::atoi(e) : (sizeof(Real) == 4 ? 4 : 1);
-    }
-    if (cols_ <= 0) {
-        const char* e = std::getenv("TOMO_COLS");
-        cols_ = e ? std::atoi(e) : 1;
-    }
-    if (!advance_kernel_for<Real>(T_, cols_, advance_mode(pc.spec)))
+    // blocking: explicit spec values, else the environment, else autotuned per batch size
+    auto env = [](const char* n) {
+        const char* e = std::getenv(n);
+        return e ? std::atoi(e) : 0;
+    };
+    fix_T_ = pc.spec.steps_per_launch > 0 ? pc.spec.steps_per_launch : env("TOMO_T");
+    fix_cols_ = pc.spec.cols_per_lane > 0 ? pc.spec.cols_per_lane : env("TOMO_COLS");
+    fix_minb_ = env("TOMO_MINB");
+    auto_T_ = fix_T_ <= 0;
+    auto_cols_ = fix_cols_ <= 0;
+    auto_minb_ = fix_minb_ <= 0;
+    const std::vector<Blocking> c = tune_candidates<Real>(advance_mode(pc.spec), std::max(fix_T_, 0),
+                                                          std::max(fix_cols_, 0), std::max(fix_minb_, 0));
+    if (c.empty())
         return fail(TOMO_EINVAL, "unsupported (steps_per_launch, cols_per_lane) pair for this mode and precision");
+    blk_ = c.front();   // until the first batch is tuned
+    return TOMO_OK;
+}
+
+// Autotuner: times every offered blocking (T, COLS, MINB) on the actual batch
+// -- its materials, descriptors and state -- and keeps the fastest per batch
+// size.  Every blocking computes the same bits, so the choice affects speed
+// only.  Each blocking runs one warm-up launch and then about kTuneSteps time
+// steps from step 0 (the descriptors are re-uploaded before each); the time
+// per step (CUDA events around the timed launches) decides.  forward() then
+// sets the state up again from scratch, so tuning leaves no trace in results.
+template <typename Real>
+int EngineT<Real>::autotune(size_t ncand) {
+    constexpr int kTuneSteps = 16;
+    const ProblemClass& pc = cd_.pc;
+    const int mode = advance_mode(pc.spec);
+    const std::vector<Blocking> cands =
+        tune_candidates<Real>(mode, std::max(fix_T_, 0), std::max(fix_cols_, 0), std::max(fix_minb_, 0));
+    if (cands.empty()) return fail(TOMO_EINVAL, "no blocking to tune");
+    const int key = (int)ncand * pc.n_exc;
+    stats_.tune_ms = 0;
+    stats_.tuned_configs = 0;
+    int maxT = 1;
+    for (const Blocking& c : cands) maxT = std::max(maxT, c.T);
+    // too few time steps to time every blocking inside the time loop: keep the default
+    if (cands.size() <= 1 || pc.S < (1 + std::max(2, kTuneSteps / maxT)) * maxT + maxT) {
+        tuned_[key] = blk_ = cands.front();
+        return TOMO_OK;
+    }
+    blk_ = cands.front();
+    TOMO_TRY(ensure_batch((int)ncand));
+    const int nsolves = nsolves_;
+    TOMO_TRY(d_upload_.ensure(sizeof(double) * up_.upload.size()));
+    int64_t kernels = 0, h2d = 0;
+    TOMO_TRY(setup_materials<Real>(cd_, up_, d_upload_.as<double>(), d_mats_.as<uint8_t>(), d_tabs_.as<Real>(), stream_,
+                                   &kernels, &h2d));
+    CUDA_TRY(cudaMemsetAsync(d_state_.p, 0, (size_t)nsolves * cd_.lay.per_solve * sizeof(Real), stream_));
+    h_descs_.resize(nsolves);
+    fill_descs<Real>(cd_, up_, d_state_.as<Real>(), d_mats_.as<uint8_t>(), d_tabs_.as<Real>(), h_descs_.data());
+    double best = 1e300;
+    Blocking bestb = cands.front();
+    std::vector<WorkItem> items;
+    for (const Blocking& c : cands) {
+        items.clear();
+        append_items(items, 0, nsolves, pc.nx, c.T, c.cols);
+        TOMO_TRY(d_tune_items_.ensure(sizeof(WorkItem) * items.size()));
+        CUDA_TRY(cudaMemcpyAsync(d_tune_items_.p, items.data(), sizeof(WorkItem) * items.size(), cudaMemcpyHostToDevice,
+                                 stream_));
+        CUDA_TRY(cudaMemcpyAsync(d_descs_.p, h_descs_.data(), sizeof(SolveDesc<Real>) * nsolves,
+                                 cudaMemcpyHostToDevice, stream_));
+        int blocks = 0;
+        size_t smem = 0;
+        TOMO_TRY(advance_grid<Real>(c, mode, (int)items.size(), num_sms_, &blocks, &smem));
+        const int L = std::max(2, kTuneSteps / c.T);
+        launch_advance<Real>(c, mode, blocks, smem, d_descs_.as<SolveDesc<Real>>(), d_tune_items_.as<WorkItem>(),
+                             (int)items.size(), nsolves, d_counter_.as<int>(), stream_);
+        CUDA_TRY(cudaEventRecord(ev_[1], stream_));
+        for (int l = 0; l < L; ++l)
+            launch_advance<Real>(c, mode, blocks, smem, d_descs_.as<SolveDesc<Real>>(), d_tune_items_.as<WorkItem>(),
+                                 (int)items.size(), nsolves, d_counter_.as<int>(), stream_);
+        CUDA_TRY(cudaEventRecord(ev_[2], stream_));
+        CUDA_TRY(cudaStreamSynchronize(stream_));
+        CUDA_TRY(cudaGetLastError());
+        float ms = 0;
+        CUDA_TRY(cudaEventElapsedTime(&ms, ev_[1], ev_[2]));
+        stats_.tune_ms += ms;
+        ++stats_.tuned_configs;
+        const double per_step = ms / (double)(L * c.T);
+        if (per_step < best) {
+            best = per_step;
+            bestb = c;
+        }
+    }
+    tuned_[key] = blk_ = bestb;
     return TOMO_OK;
 }
 
@@ -498,8 +596,9 @@ int EngineT<Real>::ensure_batch(int ncand) {
         cap_cand_ = ncand;
     }
     std::vector<WorkItem> items;
-    append_items(items, 0, nsolves, pc.nx, T_, cols_);
-    if (nsolves != nsolves_ || (int)items.size() != nitems_ || ncand != cur_cand_) {
+    append_items(items, 0, nsolves, pc.nx, blk_.T, blk_.cols);
+    if (nsolves != nsolves_ || (int)items.size() != nitems_ || ncand != cur_cand_ || blk_.T != items_blk_.T ||
+        blk_.cols != items_blk_.cols) {
         invalidate_graph();
         TOMO_TRY(d_items_.ensure(sizeof(WorkItem) * items.size()));
         CUDA_TRY(cudaMemcpyAsync(d_items_.p, items.data(), sizeof(WorkItem) * items.size(), cudaMemcpyHostToDevice,
@@ -508,21 +607,22 @@ int EngineT<Real>::ensure_batch(int ncand) {
     nsolves_ = nsolves;
     nitems_ = (int)items.size();
     cur_cand_ = ncand;
+    items_blk_ = blk_;
     return TOMO_OK;
 }
 
 template <typename Real>
 int EngineT<Real>::build_graph(int nlaunch) {
-    if (graph_exec_ && graph_cand_ == cur_cand_ && graph_T_ == T_ && graph_cols_ == cols_ && graph_launches_ == nlaunch)
+    if (graph_exec_ && graph_cand_ == cur_cand_ && graph_blk_ == blk_ && graph_launches_ == nlaunch)
         return TOMO_OK;
     invalidate_graph();
     int blocks = 0;
     size_t smem = 0;
-    TOMO_TRY(advance_grid<Real>(T_, cols_, advance_mode(cd_.pc.spec), nitems_, num_sms_, &blocks, &smem));
+    TOMO_TRY(advance_grid<Real>(blk_, advance_mode(cd_.pc.spec), nitems_, num_sms_, &blocks, &smem));
     cudaGraph_t graph;
     CUDA_TRY(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
     for (int l = 0; l < nlaunch; ++l)
-        launch_advance<Real>(T_, cols_, advance_mode(cd_.pc.spec), blocks, smem, d_descs_.as<SolveDesc<Real>>(),
+        launch_advance<Real>(blk_, advance_mode(cd_.pc.spec), blocks, smem, d_descs_.as<SolveDesc<Real>>(),
                              d_items_.as<WorkItem>(), nitems_, nsolves_, d_counter_.as<int>(), stream_);
     cudaError_t ce = cudaStreamEndCapture(stream_, &graph);
     if (ce != cudaSuccess) return fail(TOMO_ECUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
@@ -532,7 +632,7 @@ int EngineT<Real>::build_graph(int nlaunch) {
         graph_exec_ = nullptr;
         return fail(TOMO_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce));
     }
-    graph_cand_ = cur_cand_; graph_T_ = T_; graph_cols_ = cols_; graph_launches_ = nlaunch; graph_blocks_ = blocks;
+    graph_cand_ = cur_cand_; graph_blk_ = blk_; graph_launches_ = nlaunch; graph_blocks_ = blocks;
     return TOMO_OK;
 }
 
@@ -543,6 +643,16 @@ int EngineT<Real>::forward(const double* args, size_t ncand, size_t nparam, cons
     const bool want_fit = out && out->fitness;
     if (want_fit && !cd_.have_target) return fail(TOMO_ENOTARGET, "fitness needs a target (tomo_set_target)");
     TOMO_TRY(unpack_args(pc, args, ncand, nparam, up_));
+    stats_.tune_ms = 0;
+    stats_.tuned_configs = 0;
+    if ((auto_T_ || auto_cols_ || auto_minb_) && !s.plain) {
+        auto it = tuned_.find((int)ncand * pc.n_exc);
+        if (it != tuned_.end()) {
+            blk_ = it->second;
+        } else {
+            TOMO_TRY(autotune(ncand));
+        }
+    }
     TOMO_TRY(ensure_batch((int)ncand));
     const int nsolves = nsolves_;
     int64_t kernels = 0, h2d = 0, d2h = 0;
@@ -562,22 +672,18 @@ int EngineT<Real>::forward(const double* args, size_t ncand, size_t nparam, cons
     h2d += sizeof(SolveDesc<Real>) * nsolves;
 
     // time loop: ceil(S/T) advance launches + progress bumps, replayed as one CUDA graph
-    const int nlaunch = (pc.S + T_ - 1) / T_;
+    const int nlaunch = (pc.S + blk_.T - 1) / blk_.T;
     if (s.plain) {
-        // plain baseline path: every solve on its own, one launch per time step, no graph
-        std::vector<WorkItem> one;
-        append_items(one, 0, 1, pc.nx, T_, cols_);
-        const int per = (int)one.size();
-        int blocks = 0;
-        size_t smem = 0;
-        TOMO_TRY(advance_grid<Real>(T_, cols_, advance_mode(s), per, num_sms_, &blocks, &smem));
+        // plain baseline path: one solve per launch, one launch per field update
+        // and time step (H, E, DFT), no temporal blocking, no graph
+        const int ncont = pc.nfreq > 0 ? pc.C : 0;
         CUDA_TRY(cudaEventRecord(ev_[1], stream_));
         for (int sv = 0; sv < nsolves; ++sv)
-            for (int l = 0; l < nlaunch; ++l)
-                launch_advance<Real>(T_, cols_, advance_mode(s), blocks, smem, d_descs_.as<SolveDesc<Real>>() + sv,
-                                     d_items_.as<WorkItem>(), per, 1, d_counter_.as<int>(), stream_);
+            for (int n = 0; n < pc.S; ++n)
+                kernels += launch_plain_step<Real>(advance_mode(s), d_descs_.as<SolveDesc<Real>>() + sv, n, s.nx, s.ny,
+                                                   ncont, stream_);
         CUDA_TRY(cudaEventRecord(ev_[2], stream_));
-        kernels += 2 * (int64_t)nlaunch * nsolves;
+        CUDA_TRY(cudaGetLastError());
     } else {
         TOMO_TRY(build_graph(nlaunch));
         CUDA_TRY(cudaEventRecord(ev_[1], stream_));
@@ -635,10 +741,11 @@ int EngineT<Real>::forward(const double* args, size_t ncand, size_t nparam, cons
     stats_.advance_ms = adv;
     stats_.total_ms = tot;
     stats_.cell_updates = (double)nsolves * (double)s.nx * (double)s.ny * (double)pc.S;
-    stats_.launches = nlaunch;
+    stats_.launches = s.plain ? (int64_t)pc.S * nsolves : nlaunch;
     stats_.kernels = kernels;
-    stats_.steps_per_launch = T_;
-    stats_.cols_per_lane = cols_;
+    stats_.steps_per_launch = blk_.T;
+    stats_.cols_per_lane = blk_.cols;
+    stats_.min_blocks_per_sm = blk_.minb;
     stats_.h2d_bytes = h2d;
     stats_.d2h_bytes = d2h;
     if (flag && s.mode != TOMO_MODE_REFERENCE_GPU) return fail(TOMO_ENUMERIC, "non-finite field or fitness detected");

@@ -26,6 +26,7 @@ extern thread_local std::string g_last_error;
 
 int spec_reference(tomo_spec* s, int cpu_variant);
 int spec_breast(tomo_spec* s, int config);
+int spec_serving(tomo_spec* s, int edge, int n_antennas);
 int num_params(const tomo_spec* s);
 int num_excitations(const tomo_spec* s);
 int create_engine(const tomo_spec* spec, EngineBase** out);

@@ -7,7 +7,9 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <map>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/tomography.h"
@@ -97,10 +99,18 @@ struct Unpacked {
 };
 int unpack_args(const ProblemClass& pc, const double* args, size_t ncand, size_t nparam, Unpacked& u);
 
+// Blocking of the advance kernel: time steps per launch, columns per lane, and
+// the minimum resident blocks per SM its registers were allocated for.
+struct Blocking {
+    int T = 1, cols = 1, minb = 2;
+    bool operator==(const Blocking& o) const { return T == o.T && cols == o.cols && minb == o.minb; }
+    bool operator!=(const Blocking& o) const { return !(*this == o); }
+};
+
 template <typename Real>
 using AdvanceFn = void (*)(const SolveDesc<Real>*, const WorkItem*, int, int*);
 template <typename Real>
-AdvanceFn<Real> advance_kernel_for(int T, int cols, int mode);
+AdvanceFn<Real> advance_kernel_for(const Blocking& b, int mode);
 
 inline int advance_mode(const tomo_spec& s) { return s.mode == TOMO_MODE_BREAST ? kModeBreast : kModeRef; }
 template <typename Real>
@@ -295,10 +305,10 @@ int post_range(const ClassData<Real>& cd, size_t ncand, const SolveDesc<Real>& f
 
 // Grid size of the persistent advance kernel.
 template <typename Real>
-int advance_grid(int T, int cols, int mode, int nitems, int num_sms, int* blocks, size_t* smem) {
-    AdvanceFn<Real> fn = advance_kernel_for<Real>(T, cols, mode);
+int advance_grid(const Blocking& b, int mode, int nitems, int num_sms, int* blocks, size_t* smem) {
+    AdvanceFn<Real> fn = advance_kernel_for<Real>(b, mode);
     if (!fn) return fail(TOMO_EINVAL, "unsupported (steps_per_launch, cols_per_lane) pair");
-    *smem = advance_smem_bytes<Real>(T, cols);
+    *smem = advance_smem_bytes<Real>(b.T, b.cols);
     CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem));
     int per_sm = 0;
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 128, *smem));
@@ -307,12 +317,34 @@ int advance_grid(int T, int cols, int mode, int nitems, int num_sms, int* blocks
     return TOMO_OK;
 }
 
+// Blockings the autotuner times, restricted to a fixed T or COLS when nonzero
+// and to a fixed MINB when nonzero; the first entry is the default before the
+// first batch is tuned.
 template <typename Real>
-void launch_advance(int T, int cols, int mode, int blocks, size_t smem, const SolveDesc<Real>* descs,
+std::vector<Blocking> tune_candidates(int mode, int fixT, int fixCols, int fixMinb) {
+    static const int pref[][3] = {{2, 2, 2}, {2, 1, 3}, {2, 2, 3}, {2, 1, 2}, {2, 1, 4}, {4, 1, 2}, {4, 1, 3},
+                                  {4, 2, 2}, {1, 1, 2}, {1, 1, 4}, {6, 1, 2}, {8, 1, 2}};
+    std::vector<Blocking> out;
+    for (const auto& p : pref) {
+        if ((fixT && p[0] != fixT) || (fixCols && p[1] != fixCols) || (fixMinb && p[2] != fixMinb)) continue;
+        const Blocking b{p[0], p[1], p[2]};
+        if (advance_kernel_for<Real>(b, mode)) out.push_back(b);
+    }
+    return out;
+}
+
+// One time step of one solve on the plain path (H, E and DFT kernels; the DFT
+// kernel only when n_contour > 0).  Returns the number of kernels launched.
+template <typename Real>
+int launch_plain_step(int mode, const SolveDesc<Real>* d, int n, int nx, int ny, int n_contour, cudaStream_t st);
+
+template <typename Real>
+void launch_advance(const Blocking& b, int mode, int blocks, size_t smem, const SolveDesc<Real>* descs,
                     const WorkItem* items, int nitems, int nsolves, int* counter, cudaStream_t st) {
-    AdvanceFn<Real> fn = advance_kernel_for<Real>(T, cols, mode);
+    AdvanceFn<Real> fn = advance_kernel_for<Real>(b, mode);
     fn<<<blocks, 128, smem, st>>>(descs, items, nitems, counter);
-    bump_kernel<Real><<<(nsolves + 127) / 128, 128, 0, st>>>(const_cast<SolveDesc<Real>*>(descs), nsolves, T, counter);
+    bump_kernel<Real><<<(nsolves + 127) / 128, 128, 0, st>>>(const_cast<SolveDesc<Real>*>(descs), nsolves, b.T,
+                                                            counter);
 }
 
 // Work items (solve, strip) for nsolves solves starting at solve index first:
@@ -359,6 +391,7 @@ class EngineT : public EngineBase {
    private:
     int ensure_batch(int ncand);
     int build_graph(int nlaunch);
+    int autotune(size_t ncand);
     void invalidate_graph() {
         if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
         graph_exec_ = nullptr;
@@ -371,7 +404,12 @@ class EngineT : public EngineBase {
     bool own_stream_ = false;
     cudaEvent_t ev_[4] = {nullptr, nullptr, nullptr, nullptr};
     int num_sms_ = 0;
-    int T_ = 1, cols_ = 1;
+    Blocking blk_;                                 // blocking of the next batch
+    bool auto_T_ = false, auto_cols_ = false, auto_minb_ = false;   // tuned per batch size on first use
+    int fix_T_ = 0, fix_cols_ = 0, fix_minb_ = 0;  // dimensions fixed by the spec or the environment
+    std::map<int, Blocking> tuned_;                // solves per batch -> blocking
+    Blocking items_blk_{-1, -1, -1};               // blocking the uploaded work items were cut for
+    DevBuf d_tune_items_;
     uint64_t budget_ = (uint64_t)150 << 30;
     tomo_stats stats_{};
     // batch buffers
@@ -381,7 +419,8 @@ class EngineT : public EngineBase {
     Unpacked up_;
     std::vector<SolveDesc<Real>> h_descs_;
     cudaGraphExec_t graph_exec_ = nullptr;
-    int graph_cand_ = -1, graph_T_ = -1, graph_cols_ = -1, graph_launches_ = -1, graph_blocks_ = 0;
+    int graph_cand_ = -1, graph_launches_ = -1, graph_blocks_ = 0;
+    Blocking graph_blk_{-1, -1, -1};
     // serving
     ServeStateT<Real>* serve_ = nullptr;
 };

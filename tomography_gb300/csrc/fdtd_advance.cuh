@@ -94,8 +94,12 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
-constexpr int kPrefetch = 7;       // rows in flight ahead of the one being consumed
-constexpr int kRowSlots = 8;       // ring slots per warp (kPrefetch + 1)
+// Rows in flight ahead of the one being consumed.  A warp spends about a
+// microsecond per row-iteration at full occupancy, so three rows ahead cover
+// the HBM latency; the short ring keeps the shared memory of a 4-warp block
+// small enough for three or more resident blocks per SM.
+constexpr int kPrefetch = 3;
+constexpr int kRowSlots = 4;       // ring slots per warp (kPrefetch + 1, a power of two)
 
 // Kahan-compensated accumulation (FP32); plain accumulation in FP64.
 template <typename Real>
@@ -229,16 +233,18 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, 
     wdisp = __any_sync(0xffffffffu, wdisp);
 
     // rows that need the general path: CPML rows and boundaries, NTFF face rows,
-    // the source row, receiver rows, plane-wave rows (reference modes)
+    // plane-wave rows (reference modes), and -- only in the strips whose columns
+    // (halo included) hold them -- the source row and receiver rows
     uint32_t* rowbits = sm.rowbits[wib];
     const int nwords = (ny + 1 + 31) >> 5;
+    const bool src_here = psrc && src_x >= xs && src_x < xs + P;
     for (int w = lane; w < nwords; w += 32) {
         uint32_t bits = 0;
         for (int b = 0; b < 32; ++b) {
             const int m = 32 * w + b;
             bool sp = m <= nc || m >= ny - nc;
             sp |= nfreq > 0 && (m == fd + 1 || m == ny - fd);
-            sp |= psrc && m == src_y;
+            sp |= src_here && m == src_y;
             sp |= kRef && wdisp && m >= jy0 && m <= jy1;
             if (sp) bits |= 1u << b;
         }
@@ -246,8 +252,8 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, 
     }
     __syncwarp();
     for (int rr = lane; rr < D.nrx; rr += 32) {
-        const int m = D.rx[2 * rr + 1];
-        atomicOr(&rowbits[m >> 5], 1u << (m & 31));
+        const int x = D.rx[2 * rr], m = D.rx[2 * rr + 1];
+        if (x >= xs && x < xs + P) atomicOr(&rowbits[m >> 5], 1u << (m & 31));
     }
     __syncwarp();
 
@@ -688,16 +694,15 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, 
     __syncwarp();
 }
 
-#ifndef TOMO_ADVANCE_MINB
-#define TOMO_ADVANCE_MINB 1   // minimum resident blocks per SM requested from ptxas
-#endif
-
 // Persistent kernel: warps take work items from a global counter (reset by the
-// progress kernel after every launch), most expensive items first.
-template <typename Real, int T, int COLS, int MODE>
-__global__ void __launch_bounds__(128, TOMO_ADVANCE_MINB) fdtd_advance_kernel(const SolveDesc<Real>* __restrict__ descs,
-                                                          const WorkItem* __restrict__ items, int nitems,
-                                                          int* __restrict__ counter) {
+// progress kernel after every launch), most expensive items first.  MINB is
+// the minimum number of resident 128-thread blocks per SM requested from the
+// register allocator (2: up to 255 registers per thread, 3: 168, 4: 128); the
+// autotuner picks it with (T, COLS).
+template <typename Real, int T, int COLS, int MODE, int MINB>
+__global__ void __launch_bounds__(128, MINB) fdtd_advance_kernel(const SolveDesc<Real>* __restrict__ descs,
+                                                                  const WorkItem* __restrict__ items, int nitems,
+                                                                  int* __restrict__ counter) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     AdvanceSmem<Real, T, COLS>& sm = *reinterpret_cast<AdvanceSmem<Real, T, COLS>*>(smem_raw);
     const int wib = threadIdx.x >> 5;

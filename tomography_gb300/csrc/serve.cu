@@ -72,6 +72,7 @@ struct ServeStateT {
     int nitems = 0, blocks = 0;
     size_t smem = 0;
     int hi_slot = 0;   // one past the highest slot ever used
+    Blocking blk{0, 0, 0};   // blocking of the serving loop, fixed at the first serving step
 
     int find_range(int n) {
         int run = 0;
@@ -269,6 +270,7 @@ int EngineT<Real>::serve_step(int* n_active) {
     int rc;
     ServeStateT<Real>* st = serve_state(serve_, &rc);
     if (!st) return rc;
+    if (st->blk.T == 0) st->blk = blk_;   // the blocking stays fixed while requests are in flight
     // 1. admit queued requests in arrival order
     while (!st->queue.empty()) {
         auto it = st->reqs.find(st->queue.front());
@@ -292,14 +294,14 @@ int EngineT<Real>::serve_step(int* n_active) {
         std::vector<WorkItem> items;
         for (auto& kv : st->reqs) {
             const ServeRequest<Real>& r = *kv.second;
-            if (r.state == kRunning) append_items(items, r.first, r.nsolves, r.cd->pc.nx, T_, cols_);
+            if (r.state == kRunning) append_items(items, r.first, r.nsolves, r.cd->pc.nx, st->blk.T, st->blk.cols);
         }
         st->nitems = (int)items.size();
         if (!items.empty()) {
             TOMO_TRY(st->items.ensure(sizeof(WorkItem) * items.size()));
             CUDA_TRY(cudaMemcpyAsync(st->items.p, items.data(), sizeof(WorkItem) * items.size(), cudaMemcpyHostToDevice,
                                      stream_));
-            TOMO_TRY(advance_grid<Real>(T_, cols_, advance_mode(cd_.pc.spec), st->nitems, num_sms_, &st->blocks,
+            TOMO_TRY(advance_grid<Real>(st->blk, advance_mode(cd_.pc.spec), st->nitems, num_sms_, &st->blocks,
                                         &st->smem));
         }
         // the upload vectors must outlive the async copies above
@@ -309,14 +311,14 @@ int EngineT<Real>::serve_step(int* n_active) {
     // 3. one advance launch over everything admitted
     int running = 0;
     if (st->nitems > 0) {
-        launch_advance<Real>(T_, cols_, advance_mode(cd_.pc.spec), st->blocks, st->smem,
+        launch_advance<Real>(st->blk, advance_mode(cd_.pc.spec), st->blocks, st->smem,
                              st->descs.template as<SolveDesc<Real>>(), st->items.template as<WorkItem>(), st->nitems,
                              st->hi_slot, d_counter_.as<int>(), stream_);
         CUDA_TRY(cudaGetLastError());
         for (auto& kv : st->reqs) {
             ServeRequest<Real>& r = *kv.second;
             if (r.state != kRunning) continue;
-            r.steps_done += T_;
+            r.steps_done += st->blk.T;
             if (r.steps_done >= r.cd->pc.S) TOMO_TRY(retire(st, r, stream_, true));
             else ++running;
         }

@@ -1,0 +1,246 @@
+"""Synchronous particle-swarm and differential-evolution drivers over whole
+generations.
+
+The reference hands its fitness function to tao's searches as a function
+pointer (test.cxx:82-121): ``ParticleSwarmMPI ps(min_bound, max_bound,
+arguments); ps.go(FDTD_GPU)``, ``DifferentialEvolutionMPI de(...);
+de.go(...)``, with tao farming one candidate per MPI rank and call.  tao itself
+is an un-vendored submodule, so these drivers restate the textbook synchronous
+algorithms with the same construction and ``go(f)`` call shape, and evaluate
+every generation in ONE call: ``f`` receives the whole population as an
+``[n, n_param]`` array (``Solver.fitness_batch``), so all candidate x
+transmitter solves of a generation advance together on the GPU.  A
+per-candidate function of the reference's type (``FDTD_GPU(vector) ->
+double``) is accepted too with ``batch=False``.
+
+Fitness is maximised (the reference's fitness is a negative misfit).
+
+Command line (the analogue of the reference's ``--search_type ps|de``)::
+
+    python -m tomography_gb300.search --search_type ps --workload 1 \\
+        --population_size 64 --maximum_iterations 20
+"""
+from __future__ import annotations
+
+import argparse
+import dataclasses
+import json
+import sys
+import time
+from typing import Callable, Sequence
+
+import numpy as np
+
+FitnessFn = Callable[[np.ndarray], np.ndarray]
+
+
+@dataclasses.dataclass
+class SearchResult:
+    best_fitness: float
+    best_params: np.ndarray
+    history: list            # best fitness after every generation
+    evaluations: int         # candidates evaluated
+    generations: int
+    seconds: float
+
+
+def get_argument(arguments: Sequence[str] | None, name: str, default, cast=float):
+    """``--name value`` from an argv-style list (undvc_common's get_argument shape)."""
+    if arguments:
+        args = list(arguments)
+        for i, a in enumerate(args[:-1]):
+            if a == name:
+                return cast(args[i + 1])
+    return default
+
+
+class _Search:
+    def __init__(self, min_bound, max_bound, arguments=None, *, population_size=None, maximum_iterations=None,
+                 seed=None):
+        self.lo = np.asarray(min_bound, dtype=np.float64)
+        self.hi = np.asarray(max_bound, dtype=np.float64)
+        if self.lo.shape != self.hi.shape or self.lo.ndim != 1:
+            raise ValueError("min_bound and max_bound must be equal-length vectors")
+        if np.any(self.hi < self.lo):
+            raise ValueError("max_bound below min_bound")
+        self.n_param = self.lo.size
+        self.population_size = int(population_size or get_argument(arguments, "--population_size", 50, int))
+        self.maximum_iterations = int(maximum_iterations or get_argument(arguments, "--maximum_iterations", 100, int))
+        if self.population_size < 4:
+            raise ValueError("population_size must be at least 4")
+        seed = seed if seed is not None else get_argument(arguments, "--seed", 0x70F00001, int)
+        self.rng = np.random.Generator(np.random.PCG64(seed))
+        self.span = self.hi - self.lo
+
+    def _uniform(self, n: int) -> np.ndarray:
+        return self.lo + self.rng.random((n, self.n_param)) * self.span
+
+    def _clip(self, x: np.ndarray) -> np.ndarray:
+        return np.clip(x, self.lo, self.hi)
+
+    @staticmethod
+    def _evaluator(f, batch: bool) -> FitnessFn:
+        if batch:
+            def ev(x):
+                out = np.asarray(f(np.ascontiguousarray(x)), dtype=np.float64).reshape(-1)
+                if out.size != x.shape[0]:
+                    raise ValueError(f"fitness function returned {out.size} values for {x.shape[0]} candidates")
+                return out
+            return ev
+        return lambda x: np.array([float(f(list(row))) for row in x], dtype=np.float64)
+
+
+class ParticleSwarm(_Search):
+    """Synchronous global-best particle swarm.
+
+    v <- w v + c1 r1 (p_best - x) + c2 r2 (g_best - x);  x <- clip(x + v).
+    ``--inertia``, ``--local_best_weight``, ``--global_best_weight`` as in tao's
+    particle swarm arguments."""
+
+    def __init__(self, min_bound, max_bound, arguments=None, *, inertia=None, local_best_weight=None,
+                 global_best_weight=None, **kw):
+        super().__init__(min_bound, max_bound, arguments, **kw)
+        self.inertia = float(inertia if inertia is not None else get_argument(arguments, "--inertia", 0.75))
+        self.c1 = float(local_best_weight if local_best_weight is not None
+                        else get_argument(arguments, "--local_best_weight", 1.5))
+        self.c2 = float(global_best_weight if global_best_weight is not None
+                        else get_argument(arguments, "--global_best_weight", 1.5))
+
+    def go(self, f, batch: bool = True, callback=None) -> SearchResult:
+        ev = self._evaluator(f, batch)
+        t0 = time.perf_counter()
+        n = self.population_size
+        x = self._uniform(n)
+        v = (self.rng.random((n, self.n_param)) * 2.0 - 1.0) * self.span * 0.1
+        fx = ev(x)
+        pbest, pfit = x.copy(), fx.copy()
+        g = int(np.argmax(pfit))
+        gbest, gfit = pbest[g].copy(), float(pfit[g])
+        history = [gfit]
+        evals = n
+        for it in range(self.maximum_iterations):
+            r1 = self.rng.random((n, self.n_param))
+            r2 = self.rng.random((n, self.n_param))
+            v = self.inertia * v + self.c1 * r1 * (pbest - x) + self.c2 * r2 * (gbest - x)
+            x = self._clip(x + v)
+            fx = ev(x)
+            evals += n
+            better = fx > pfit
+            pbest[better] = x[better]
+            pfit[better] = fx[better]
+            g = int(np.argmax(pfit))
+            if pfit[g] > gfit:
+                gbest, gfit = pbest[g].copy(), float(pfit[g])
+            history.append(gfit)
+            if callback:
+                callback(it, gfit, gbest)
+        return SearchResult(gfit, gbest, history, evals, self.maximum_iterations, time.perf_counter() - t0)
+
+
+class DifferentialEvolution(_Search):
+    """Synchronous differential evolution, DE/{best,random}/k/bin.
+
+    Donor = parent + F * sum_k (x_a_k - x_b_k) over ``--number_pairs`` pairs of
+    distinct other members; binomial crossover at ``--crossover_rate`` with at
+    least one donor gene; the trial replaces its target when it is not worse."""
+
+    def __init__(self, min_bound, max_bound, arguments=None, *, crossover_rate=None, differential_scale=None,
+                 number_pairs=None, parent_selection=None, **kw):
+        super().__init__(min_bound, max_bound, arguments, **kw)
+        self.cr = float(crossover_rate if crossover_rate is not None
+                        else get_argument(arguments, "--crossover_rate", 0.5))
+        self.F = float(differential_scale if differential_scale is not None
+                       else get_argument(arguments, "--differential_scale", 0.5))
+        self.pairs = int(number_pairs if number_pairs is not None else get_argument(arguments, "--number_pairs", 1, int))
+        self.parent = str(parent_selection if parent_selection is not None
+                          else get_argument(arguments, "--parent_selection", "best", str))
+        if self.parent not in ("best", "random"):
+            raise ValueError("parent_selection must be 'best' or 'random'")
+        if self.population_size < 2 * self.pairs + 2:
+            raise ValueError("population too small for the number of difference pairs")
+
+    def go(self, f, batch: bool = True, callback=None) -> SearchResult:
+        ev = self._evaluator(f, batch)
+        t0 = time.perf_counter()
+        n, p = self.population_size, self.n_param
+        x = self._uniform(n)
+        fx = ev(x)
+        history = [float(fx.max())]
+        evals = n
+        for it in range(self.maximum_iterations):
+            best = int(np.argmax(fx))
+            trial = np.empty_like(x)
+            for i in range(n):
+                others = [j for j in range(n) if j != i]
+                pick = self.rng.choice(others, size=2 * self.pairs, replace=False)
+                base = x[best] if self.parent == "best" else x[int(self.rng.choice(others))]
+                donor = base.copy()
+                for k in range(self.pairs):
+                    donor += self.F * (x[pick[2 * k]] - x[pick[2 * k + 1]])
+                mask = self.rng.random(p) < self.cr
+                mask[self.rng.integers(p)] = True
+                trial[i] = np.where(mask, donor, x[i])
+            trial = self._clip(trial)
+            ft = ev(trial)
+            evals += n
+            keep = ft >= fx
+            x[keep] = trial[keep]
+            fx[keep] = ft[keep]
+            history.append(float(fx.max()))
+            if callback:
+                callback(it, history[-1], x[int(np.argmax(fx))])
+        b = int(np.argmax(fx))
+        return SearchResult(float(fx[b]), x[b].copy(), history, evals, self.maximum_iterations,
+                            time.perf_counter() - t0)
+
+
+def breast_bounds(n_ellipses: int, disc_radius: float):
+    """Per-parameter bounds of the breast-imaging candidates: 8 per ellipse
+    (cx, cy, a, b, angle, eps_inf, delta_eps, sigma)."""
+    lo = np.tile([-disc_radius, -disc_radius, 2e-3, 2e-3, 0.0, 2.0, 1.0, 0.0], n_ellipses)
+    hi = np.tile([disc_radius, disc_radius, 15e-3, 15e-3, np.pi, 20.0, 40.0, 1.0], n_ellipses)
+    return lo, hi
+
+
+def reference_bounds():
+    """test.cxx:60-77: eps_inf in [1, 7], delta_eps in [1.5, 41], sigma fixed at 0 for the 3x3 patches."""
+    lo = np.array([1.0] * 9 + [1.5] * 9 + [0.0] * 9)
+    hi = np.array([7.0] * 9 + [41.0] * 9 + [0.0] * 9)
+    return lo, hi
+
+
+def main(argv=None) -> int:
+    argv = list(sys.argv[1:] if argv is None else argv)
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--search_type", required=True, choices=["ps", "de"])
+    ap.add_argument("--workload", type=int, default=1, help="breast-imaging workload (0..4)")
+    ap.add_argument("--target_seed_offset", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=0, help="override the time steps per solve")
+    args, rest = ap.parse_known_args(argv)
+
+    import tomography_gb300 as T
+    from tomography_gb300 import workloads as W
+
+    spec = T.breast_spec(args.workload)
+    if args.steps:
+        spec = spec.copy(steps=args.steps)
+    K = spec.n_ellipses
+    with T.Solver(spec.copy(n_ellipses=3)) as ts:
+        target = ts.forward(W.target_phantom(args.workload, 3), traces=True, far_field=False)["traces"][0]
+    lo, hi = breast_bounds(K, spec.disc_radius)
+    search = (ParticleSwarm if args.search_type == "ps" else DifferentialEvolution)(lo, hi, rest)
+    with T.Solver(spec) as s:
+        s.set_target(target)
+
+        def report(it, best, _):
+            print(json.dumps({"generation": it, "best_fitness": best}), flush=True)
+
+        res = search.go(s.fitness_batch, callback=report)
+    print(json.dumps({"search_type": args.search_type, "best_fitness": res.best_fitness,
+                      "evaluations": res.evaluations, "generations": res.generations, "seconds": res.seconds,
+                      "evals_per_s": res.evaluations / res.seconds}))
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
