@@ -57,7 +57,7 @@ typedef struct tomo_spec {
     double dt;                 /* time step [s]                                      */
     int32_t steps;             /* time steps per solve                               */
     /* CPML (FDTD_GPU.cu:748-806) */
-    int32_t ncpml;
+    int32_t ncpml;             /* CPML cells per side, 0..32                         */
     double cpml_grading, cpml_sigma_max, cpml_kappa_max, cpml_alpha_max, cpml_alpha_min;
     double tau;                /* Debye relaxation time [s]                          */
     /* reference plane-wave modes */

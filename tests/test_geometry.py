@@ -1,0 +1,54 @@
+"""CPU: the strip geometry of the advance kernel (the engine's own host code,
+through an internal export).  For every grid, blocking and CPML/NTFF layout:
+each column is owned by exactly one item; no item owns more columns than its
+layout allows; the column window of every item lies inside the zero padding
+of the field rows; wide windows start on a multiple of COLS (the row copies
+move COLS elements at once); and no wide window -- owned columns and halo --
+touches a column that needs the general path (PEC boundary, CPML, vertical
+NTFF faces)."""
+from __future__ import annotations
+
+import ctypes as C
+
+import pytest
+
+PAD_LEFT, PAD_RIGHT = 32, 160
+
+
+def _items(lib, nx, nc, d, T, cols):
+    buf = (C.c_int * 3000)()
+    n = lib.tomo_internal_work_items(nx, nc, d, T, cols, buf, 1000)
+    assert n > 0, lib.tomo_last_error()
+    return [(buf[3 * i], buf[3 * i + 1], buf[3 * i + 2]) for i in range(n)]
+
+
+@pytest.mark.parametrize("T,cols", [(1, 1), (2, 1), (2, 2), (4, 1), (4, 2), (6, 1), (8, 1)])
+def test_strip_geometry(tomo, T, cols):
+    lib = tomo.library()
+    grids = list(range(16, 140, 3)) + [200, 255, 256, 257, 400, 401, 512, 600, 601, 1024, 2048]
+    wide_seen = 0
+    for nx in grids:
+        for nc in (0, 8, 10, 12, 16, 32):
+            if 2 * nc + 4 > nx:
+                continue
+            for d in (-1, nc + 3):
+                if d >= 0 and 2 * d + 4 > nx:
+                    continue
+                owned = [0] * (nx + 1)
+                for x0, x1, narrow in _items(lib, nx, nc, d, T, cols):
+                    c = cols if (cols > 1 and not narrow) else 1
+                    P = 32 * c
+                    xs = x1 + T - P
+                    assert 0 <= x0 < x1 <= nx + 1 and x1 - x0 <= P - 2 * T
+                    assert xs <= x0 - T and xs >= -PAD_LEFT and xs + P <= nx + 1 + PAD_RIGHT
+                    assert xs % c == 0, (nx, nc, d, x0, x1)
+                    for x in range(x0, x1):
+                        owned[x] += 1
+                    if c > 1:
+                        wide_seen += 1
+                        for x in range(xs, xs + P):
+                            special = x <= nc or x >= nx - nc or (d >= 0 and x in (d, nx - d - 1))
+                            assert not special, (nx, nc, d, T, cols, x0, x1, x)
+                assert owned == [1] * (nx + 1), (nx, nc, d)
+    if cols > 1:
+        assert wide_seen > 0

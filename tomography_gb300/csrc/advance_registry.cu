@@ -24,7 +24,7 @@ AdvanceFn<double> advance_kernel_for<double>(const Blocking& b, int mode) {
 template <typename Real>
 size_t advance_smem_bytes(int T, int cols) {
 #define TOMO_SMEM(TT, CC) \
-    if (T == TT && cols == CC) return sizeof(AdvanceSmem<Real, TT, CC>);
+    if (T == TT && cols == CC) return advance_block_smem<Real, TT, CC>();
     TOMO_SMEM(1, 1)
     TOMO_SMEM(2, 1)
     TOMO_SMEM(2, 2)

@@ -184,7 +184,7 @@ int validate_spec(const tomo_spec* s) {
     if (s->nx < 16 || s->ny < 16 || s->nx > 8190 || s->ny > 8190) return fail(TOMO_EINVAL, "grid size out of range");
     if (s->steps < 1) return fail(TOMO_EINVAL, "steps must be positive");
     if (!(s->dx > 0) || !(s->dt > 0)) return fail(TOMO_EINVAL, "dx and dt must be positive");
-    if (s->ncpml < 0 || s->ncpml > 64 || 2 * s->ncpml + 4 > std::min(s->nx, s->ny))
+    if (s->ncpml < 0 || s->ncpml > kMaxCpml || 2 * s->ncpml + 4 > std::min(s->nx, s->ny))
         return fail(TOMO_EINVAL, "ncpml out of range");
     if (s->nfreq < 0 || s->nfreq > TOMO_MAX_FREQS) return fail(TOMO_EINVAL, "nfreq out of range");
     if (s->nfreq > 0 && (s->nf2ff_d < 1 || 2 * s->nf2ff_d + 4 > std::min(s->nx, s->ny)))
@@ -514,7 +514,8 @@ int EngineT<Real>::autotune(size_t ncand) {
     std::vector<WorkItem> items;
     for (const Blocking& c : cands) {
         items.clear();
-        append_items(items, 0, nsolves, pc.nx, c.T, c.cols);
+        append_items(items, 0, nsolves, pc.nx, pc.nc, item_face_distance(pc), c.T, c.cols);
+        TOMO_TRY(validate_items(items, 0, pc.nx, c.T, c.cols));
         TOMO_TRY(d_tune_items_.ensure(sizeof(WorkItem) * items.size()));
         CUDA_TRY(cudaMemcpyAsync(d_tune_items_.p, items.data(), sizeof(WorkItem) * items.size(), cudaMemcpyHostToDevice,
                                  stream_));
@@ -596,7 +597,8 @@ int EngineT<Real>::ensure_batch(int ncand) {
         cap_cand_ = ncand;
     }
     std::vector<WorkItem> items;
-    append_items(items, 0, nsolves, pc.nx, blk_.T, blk_.cols);
+    append_items(items, 0, nsolves, pc.nx, pc.nc, item_face_distance(pc), blk_.T, blk_.cols);
+    TOMO_TRY(validate_items(items, 0, pc.nx, blk_.T, blk_.cols));
     if (nsolves != nsolves_ || (int)items.size() != nitems_ || ncand != cur_cand_ || blk_.T != items_blk_.T ||
         blk_.cols != items_blk_.cols) {
         invalidate_graph();
@@ -781,3 +783,19 @@ int create_engine(const tomo_spec* spec, EngineBase** out) {
 }
 
 }  // namespace tomo
+
+// Internal test hook (not part of the public ABI): the work items the engine
+// launches for one solve of a grid, as (x0, x1, narrow) triples, after the
+// same host validation.  Returns the item count, or a negative status.
+extern "C" int tomo_internal_work_items(int nx, int ncpml, int d, int T, int cols, int* out, int cap) {
+    std::vector<tomo::WorkItem> items;
+    tomo::append_items(items, 0, 1, nx, ncpml, d, T, cols);
+    TOMO_TRY(tomo::validate_items(items, 0, nx, T, cols));
+    if (!out || (int)items.size() > cap) return tomo::fail(TOMO_EINVAL, "item buffer too small");
+    for (size_t i = 0; i < items.size(); ++i) {
+        out[3 * i] = items[i].x0;
+        out[3 * i + 1] = items[i].x1;
+        out[3 * i + 2] = items[i].narrow;
+    }
+    return (int)items.size();
+}

@@ -347,19 +347,71 @@ void launch_advance(const Blocking& b, int mode, int blocks, size_t smem, const 
                                                             counter);
 }
 
-// Work items (solve, strip) for nsolves solves starting at solve index first:
-// the edge strips (CPML, PEC boundary, vertical NTFF faces: the expensive
-// ones) of every solve first, then the interior strips.
-inline void append_items(std::vector<WorkItem>& items, int first, int nsolves, int nx, int T, int cols) {
-    const int W = 32 * cols - 2 * T;
-    const int nstrips = (nx + 1 + W - 1) / W;
-    for (int sv = 0; sv < nsolves; ++sv) {
-        items.push_back({first + sv, 0});
-        if (nstrips > 1) items.push_back({first + sv, nstrips - 1});
+// Work items of nsolves solves of a grid with nx + 1 columns, starting at
+// solve index `first`.  Columns x <= lo and x >= hi (PEC boundary, CPML,
+// vertical NTFF faces: lo = max(ncpml, d), hi = min(nx - ncpml, nx - d - 1)
+// with d the NTFF distance, or -1 without NTFF) need the general path on every
+// row.  With COLS > 1 those columns, plus the T-column halo an interior strip
+// would reach into them, go to narrow items (32 - 2T owned columns) and the
+// rest to wide items (32*COLS - 2T), so the general path runs on as few lanes
+// as possible.  The edge items of every solve come first: they cost the most.
+inline void append_items(std::vector<WorkItem>& items, int first, int nsolves, int nx, int ncpml, int d, int T,
+                         int cols) {
+    const int W1 = 32 - 2 * T, W2 = 32 * cols - 2 * T;
+    const int ncol = nx + 1;
+    std::vector<WorkItem> edge, mid;   // one solve's items (solve index filled in below)
+    const int lo = std::max(ncpml, d);
+    const int hi = d >= 0 ? std::min(nx - ncpml, nx - d - 1) : nx - ncpml;
+    // Wide items copy rows COLS elements at a time, so their column windows
+    // start at multiples of COLS: every wide-item boundary is = T (mod COLS)
+    // (the window of a full item starts at x0 - T, a clipped one at x1 + T - P).
+    const int a = (lo + 1 + T + W1 - 1) / W1 * W1;          // first interior column: a - T > lo
+    int b = ncol - (ncol - hi + T + W1 - 1) / W1 * W1;        // interior end: b - 1 + T < hi
+    b -= (((b - T) % cols) + cols) % cols;
+    const bool aligned = cols == 1 || ((a - T) % cols == 0 && (2 * T) % cols == 0);
+    if (cols == 1 || !aligned || b - a < W2) {
+        const int n = (ncol + W1 - 1) / W1;
+        for (int q = 0; q < n; ++q) {
+            const WorkItem w{0, q * W1, std::min((q + 1) * W1, ncol), cols > 1 ? 1 : 0};
+            (q == 0 || q == n - 1 ? edge : mid).push_back(w);
+        }
+    } else {
+        for (int x = 0; x < a; x += W1) edge.push_back({0, x, x + W1, 1});
+        for (int x = b; x < ncol; x += W1) edge.push_back({0, x, std::min(x + W1, ncol), 1});
+        for (int x = a; x < b; x += W2) mid.push_back({0, x, std::min(x + W2, b), 0});
     }
     for (int sv = 0; sv < nsolves; ++sv)
-        for (int q = 1; q + 1 < nstrips; ++q) items.push_back({first + sv, q});
+        for (WorkItem w : edge) {
+            w.solve = first + sv;
+            items.push_back(w);
+        }
+    for (int sv = 0; sv < nsolves; ++sv)
+        for (WorkItem w : mid) {
+            w.solve = first + sv;
+            items.push_back(w);
+        }
 }
+
+// Host check of work items before they reach the GPU: owned ranges inside the
+// grid and no wider than the layout allows, column windows inside the zero
+// padding of the field rows, and wide windows aligned for COLS-element copies.
+// A violation is a geometry bug; it fails the call instead of launching.
+inline int validate_items(const std::vector<WorkItem>& items, size_t first_item, int nx, int T, int cols) {
+    for (size_t i = first_item; i < items.size(); ++i) {
+        const WorkItem& w = items[i];
+        const int c = (cols > 1 && !w.narrow) ? cols : 1;
+        const int P = 32 * c;
+        const int xs = w.x1 + T - P;
+        if (w.x0 < 0 || w.x1 > nx + 1 || w.x1 <= w.x0 || w.x1 - w.x0 > P - 2 * T || xs > w.x0 - T ||
+            xs < -kPadLeft || xs + P > nx + 1 + kPadRight || (xs % c) != 0)
+            return fail(TOMO_ECUDA, "internal error: work item (" + std::to_string(w.x0) + ", " + std::to_string(w.x1) +
+                                        ") invalid for nx " + std::to_string(nx));
+    }
+    return TOMO_OK;
+}
+
+// NTFF distance of a class as append_items wants it (-1: no NTFF).
+inline int item_face_distance(const ProblemClass& pc) { return pc.nfreq > 0 ? pc.spec.nf2ff_d : -1; }
 
 // ------------------------------------------------------------------- engine
 template <typename Real>

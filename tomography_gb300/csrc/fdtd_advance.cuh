@@ -2,8 +2,11 @@
 //
 // Work decomposition.  A work item is one vertical strip of one solve.  One
 // warp owns the item: each lane holds COLS consecutive columns, so a warp
-// spans P = 32*COLS columns, of which the middle W = P - 2T are written back
-// (the T columns on either side are a recomputed halo).  The warp sweeps the
+// spans P = 32*COLS columns; it writes back the item's owned columns (at most
+// W = P - 2T of them) and recomputes the T columns on either side as halo.
+// Strips near the left and right edges (PEC boundary, CPML, vertical NTFF
+// faces) use the narrow COLS = 1 layout inside the same launch, so that the
+// general path below runs on as few lanes as possible.  The warp sweeps the
 // strip bottom-to-top, one row per iteration, and carries T time levels in
 // flight: level k receives row r-2k (from level k-1 one iteration earlier),
 // advances row r-2k-1 from time n0+k to n0+k+1 and hands it to level k+1.
@@ -35,9 +38,15 @@
 
 namespace tomo {
 
+// One vertical strip of one solve: owned columns [x0, x1) of solve `solve`.
+// Narrow items (COLS = 1 layout, 32 - 2T owned columns) cover the CPML,
+// boundary and vertical NTFF-face columns near the left and right edges, where
+// the general path runs on every row; wide items (the kernel's COLS) cover the
+// interior, whose halo stays clear of those columns.
 struct WorkItem {
     int solve;
-    int strip;
+    int x0, x1;
+    int narrow;
 };
 
 enum AdvanceMode : int {
@@ -153,33 +162,48 @@ __device__ __forceinline__ void load_coefs(const double* t, double& a, double& b
     a = v0.x; b = v0.y; c = v1.x; d = v1.y;
 }
 
-// Dynamic shared memory per block (4 warps).
+// Shared memory of one warp (a block holds four such regions, each sized for
+// the larger of the narrow and the wide layout).
 template <typename Real, int T, int COLS>
-struct AdvanceSmem {
-    Real rows[4][kRowSlots][4][32 * COLS];   // per-warp prefetch ring: Ez, Hx, Hy, Jp of kRowSlots rows
-    Real psring[4][kRowSlots][4][32 * COLS]; // per-warp prefetch ring: CPML psi (hyx, ezx, hxy, ezy) at time n0
-    Real pslev[4][T > 1 ? T - 1 : 1][4][4][32 * COLS];   // psi after level k, 4 rows in flight
-    Real tab[4][kMaxMat][4];                 // per-warp Ca, Cb, Cj, Bp of every material
-    Real ring[4][2][kRing][T][2];            // per-warp vertical-face DFT samples (h, e)
-    uint32_t rowbits[4][kMaxRowWords];       // per-warp "row needs the general path" flags
-    uint8_t mats[4][kRowSlots][32 * COLS + 16];   // per-warp prefetch ring: material bytes
+struct WarpSmem {
+    Real rows[kRowSlots][4][32 * COLS];   // prefetch ring: Ez, Hx, Hy, Jp of kRowSlots rows
+    Real psring[kRowSlots][4][32 * COLS]; // prefetch ring: CPML psi (hyx, ezx, hxy, ezy) at time n0
+    Real pslev[T > 1 ? T - 1 : 1][4][4][32 * COLS];   // psi after level k, 4 rows in flight
+    Real tab[kMaxMat][4];                 // Ca, Cb, Cj, Bp of every material
+    Real cpml[6 * kMaxCpml];              // CPML profile (1/ke, be, ae, 1/km, bm, am)
+    Real ring[2][kRing][T][2];            // vertical-face DFT samples (h, e)
+    uint32_t rowbits[kMaxRowWords];       // "row needs the general path" flags
+    uint8_t mats[kRowSlots][32 * COLS + 16];   // prefetch ring: material bytes
 };
 
+template <typename Real, int T, int COLS>
+constexpr size_t warp_smem_bytes() {
+    constexpr size_t a = sizeof(WarpSmem<Real, T, COLS>), b = sizeof(WarpSmem<Real, T, 1>);
+    return ((a > b ? a : b) + 15) / 16 * 16;
+}
+
+// Dynamic shared memory of a 4-warp block.
+template <typename Real, int T, int COLS>
+constexpr size_t advance_block_smem() { return 4 * warp_smem_bytes<Real, T, COLS>(); }
+
 template <typename Real, int T, int COLS, int MODE>
-__device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, AdvanceSmem<Real, T, COLS>& sm,
-                             int wib) {
+__device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkItem& wi, WarpSmem<Real, T, COLS>& ws) {
     // The descriptor is read-only for the whole launch (restrict).
     const SolveDesc<Real>& D = *Dp;
     using O = Op<Real>;
     constexpr int P = 32 * COLS;
-    constexpr int W = P - 2 * T;
+    static_assert(P > 2 * T, "a strip must own at least one column");
     constexpr bool kRef = MODE == kModeRef;
     const int lane = threadIdx.x & 31;
     const int nx = D.nx, ny = D.ny, nc = D.ncpml, S = D.steps_total, n0 = D.step;
     const int nsteps = min(T, S - n0);
     if (nsteps <= 0) return;
     const int pitch = D.pitch;
-    const int xs = strip * W - T;      // column of position 0
+    // The warp's P columns end T columns right of the owned range [x0, x1)
+    // (x1 - x0 <= P - 2T): a clipped strip carries extra halo on its left, so
+    // its columns never reach further right than a full strip ending at x1.
+    const int xs = wi.x1 + T - P;      // column of position 0
+    const int ox0 = wi.x0, ox1 = wi.x1;
     const int src = D.parity, dst = 1 - src;
     const Real chez = D.chez, Kp = D.Kp, dxr = D.dx;
     const bool clampnan = kRef && (D.flags & kNanClamp) != 0;
@@ -189,14 +213,15 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, 
     const int psy0 = 2 * (ny + 1) * 2 * nc;
     const int psy_h = psy0, psy_e = psy0 + 2 * nc * (nx + 1);         // y-strip psi sub-arrays
     const uint8_t* __restrict__ matp = D.mat;
-    const Real* __restrict__ cpml = D.cpml;
+    Real* const cpml = ws.cpml;   // CPML profile, copied to shared memory below
     const Real* __restrict__ phasor = D.phasor;
     Real* __restrict__ acc = D.acc;
     const int mpitch = D.mpitch, jx0 = D.jx0, jx1 = D.jx1, jy0 = D.jy0, jy1 = D.jy1;
     const int src_x = D.src_x, src_y = D.src_y;
 
-    // hot material coefficients -> shared memory (per warp)
-    for (int i = lane; i < kMaxMat * 4; i += 32) sm.tab[wib][i >> 2][i & 3] = D.mtab[(i >> 2) * kMatCoef + (i & 3)];
+    // hot material coefficients and the CPML profile -> shared memory (per warp)
+    for (int i = lane; i < kMaxMat * 4; i += 32) ws.tab[i >> 2][i & 3] = D.mtab[(i >> 2) * kMatCoef + (i & 3)];
+    for (int i = lane; i < 6 * nc; i += 32) cpml[i] = D.cpml[i];
 
     // per-column constants
     int xcol[COLS];
@@ -209,7 +234,7 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, 
         int x = xs + lane * COLS + c;
         xcol[c] = x;
         int pos = lane * COLS + c;
-        owned[c] = pos >= T && pos < P - T && x >= 0 && x <= nx;
+        owned[c] = x >= ox0 && x < ox1;
         ixh[c] = (x >= 0 && x < nc) ? nc - 1 - x : ((x >= nx - nc && x < nx) ? x - nx + nc : -1);
         ixe[c] = (x >= 1 && x <= nc) ? nc - x : ((x >= nx - nc && x <= nx - 1) ? x - nx + nc : -1);
         face_slot[c] = -1;
@@ -235,14 +260,15 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, 
     // rows that need the general path: CPML rows and boundaries, NTFF face rows,
     // plane-wave rows (reference modes), and -- only in the strips whose columns
     // (halo included) hold them -- the source row and receiver rows
-    uint32_t* rowbits = sm.rowbits[wib];
+    uint32_t* rowbits = ws.rowbits;
     const int nwords = (ny + 1 + 31) >> 5;
     const bool src_here = psrc && src_x >= xs && src_x < xs + P;
     for (int w = lane; w < nwords; w += 32) {
         uint32_t bits = 0;
         for (int b = 0; b < 32; ++b) {
             const int m = 32 * w + b;
-            bool sp = m <= nc || m >= ny - nc;
+            // breast mode: y-CPML rows run on the fast path (uniform psi terms)
+            bool sp = kRef ? (m <= nc || m >= ny - nc) : (m <= 0 || m >= ny);
             sp |= nfreq > 0 && (m == fd + 1 || m == ny - fd);
             sp |= src_here && m == src_y;
             sp |= kRef && wdisp && m >= jy0 && m <= jy1;
@@ -288,11 +314,11 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, 
     const Real* __restrict__ psi_src = D.psi[src];
     Real* __restrict__ psi_dst = D.psi[dst];
     auto psi_in = [&](int k, int f, int m, int c) -> Real {
-        if (k == 0) return sm.psring[wib][m & (kRowSlots - 1)][f][lane * COLS + c];
-        return sm.pslev[wib][(k - 1) % (T > 1 ? T - 1 : 1)][f][m & 3][lane * COLS + c];
+        if (k == 0) return ws.psring[m & (kRowSlots - 1)][f][lane * COLS + c];
+        return ws.pslev[(k - 1) % (T > 1 ? T - 1 : 1)][f][m & 3][lane * COLS + c];
     };
     auto psi_out = [&](int k, int f, int m, int c, Real v, size_t goff) {
-        if (k + 1 < T) sm.pslev[wib][k % (T > 1 ? T - 1 : 1)][f][m & 3][lane * COLS + c] = v;
+        if (k + 1 < T) ws.pslev[k % (T > 1 ? T - 1 : 1)][f][m & 3][lane * COLS + c] = v;
         else if (owned[c]) psi_dst[goff] = v;
     };
     bool wxs = false;   // warp holds an x-strip column (uniform)
@@ -312,14 +338,14 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, 
         const bool valid = r <= ny;
         const long long rowoff = (long long)(valid ? r : 0) * pitch;
         const int x0 = xs + lane * COLS;
-        Real* d = &sm.rows[wib][slot][0][lane * COLS];
+        Real* d = &ws.rows[slot][0][lane * COLS];
         cp_async<kBytes>(d, ez_s + rowoff + x0, valid);
         cp_async<kBytes>(d + P, hx_s + rowoff + x0, valid);
         cp_async<kBytes>(d + 2 * P, hy_s + rowoff + x0, valid);
         const bool jv = valid && r >= jy0 && r <= jy1 && x0 + COLS - 1 >= jx0 && x0 <= jx1;
         cp_async<kBytes>(d + 3 * P, jp_s + rowoff + x0, jv);
         if (lane <= P / 4)
-            cp_async<4>(&sm.mats[wib][slot][4 * lane], matp + (long long)(valid ? r : 0) * mpitch + mstart + 4 * lane,
+            cp_async<4>(&ws.mats[slot][4 * lane], matp + (long long)(valid ? r : 0) * mpitch + mstart + 4 * lane,
                         valid);
         if (wxs) {
 #pragma unroll
@@ -329,9 +355,9 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, 
                 const bool ev = valid && ixe[c] >= 0 && r >= 1 && r <= ny - 1;
                 const int xh = (x < nc) ? x : x - (nx - nc) + nc;
                 const int xe = (x <= nc) ? x - 1 : x - (nx - nc) + nc;
-                cp_async<sizeof(Real)>(&sm.psring[wib][slot][0][lane * COLS + c],
+                cp_async<sizeof(Real)>(&ws.psring[slot][0][lane * COLS + c],
                                        psi_src + (hv ? psx_h + (size_t)r * 2 * nc + xh : 0), hv);
-                cp_async<sizeof(Real)>(&sm.psring[wib][slot][1][lane * COLS + c],
+                cp_async<sizeof(Real)>(&ws.psring[slot][1][lane * COLS + c],
                                        psi_src + (ev ? psx_e + (size_t)r * 2 * nc + xe : 0), ev);
             }
         }
@@ -343,9 +369,9 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, 
                 const int x = xcol[c];
                 const bool hv = yh >= 0 && x >= 0 && x < nx;
                 const bool ev = ye >= 0 && x >= 1 && x <= nx - 1;
-                cp_async<sizeof(Real)>(&sm.psring[wib][slot][2][lane * COLS + c],
+                cp_async<sizeof(Real)>(&ws.psring[slot][2][lane * COLS + c],
                                        psi_src + (hv ? psy_h + (size_t)yh * (nx + 1) + x : 0), hv);
-                cp_async<sizeof(Real)>(&sm.psring[wib][slot][3][lane * COLS + c],
+                cp_async<sizeof(Real)>(&ws.psring[slot][3][lane * COLS + c],
                                        psi_src + (ev ? psy_e + (size_t)ye * (nx + 1) + x : 0), ev);
             }
         }
@@ -364,14 +390,14 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, 
         uint32_t lm = 0u;
         {
             const int slot = r & (kRowSlots - 1);
-            const Real* sp = &sm.rows[wib][slot][0][lane * COLS];
+            const Real* sp = &ws.rows[slot][0][lane * COLS];
 #pragma unroll
             for (int c = 0; c < COLS; ++c) {
                 lz[c] = sp[c];
                 lx[c] = sp[P + c];
                 ly[c] = sp[2 * P + c];
                 lj[c] = sp[3 * P + c];
-                lm |= (uint32_t)sm.mats[wib][slot][moff + lane * COLS + c] << (8 * c);
+                lm |= (uint32_t)ws.mats[slot][moff + lane * COLS + c] << (8 * c);
             }
         }
 
@@ -393,14 +419,26 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, 
                 const bool rowbit = (rowbits[m >> 5] >> (m & 31)) & 1u;
                 const bool fast = !wspecial && !rowbit;
                 if (k < nsteps && fast) {
-                    // ================= fast path: interior Yee + Debye
+                    // ================= fast path: interior Yee + Debye; in breast mode
+                    // also the rows of the y-CPML strips (row-uniform psi terms, the
+                    // general path's formulas; rows 0 and ny stay on the general path)
+                    const int iyh = kRef ? -1 : ((m < nc) ? nc - 1 - m : ((m >= ny - nc) ? m - ny + nc : -1));
+                    const int iye = kRef ? -1 : ((m <= nc) ? nc - m : ((m >= ny - nc) ? m - ny + nc : -1));
                     const Real ezR_last = __shfl_down_sync(0xffffffffu, pz[k][0], 1);
 #pragma unroll
                     for (int c = 0; c < COLS; ++c) {
                         const Real ez0 = pz[k][c];
                         const Real ezR = (c + 1 < COLS) ? pz[k][c + 1] : ezR_last;
                         oy[c] = O::fma(chez, O::sub(ezR, ez0), py_[k][c]);
-                        ox[c] = O::fma(-chez, O::sub(iz[c], ez0), px_[k][c]);
+                        const Real dEx = O::sub(iz[c], ez0);
+                        ox[c] = O::fma(-chez, dEx, px_[k][c]);
+                        if (iyh >= 0) {
+                            const int ysx = (m < nc) ? m : m - (ny - nc) + nc;
+                            const Real ps = O::fma(cpml[4 * nc + iyh], psi_in(k, 2, m, c), O::mul(cpml[5 * nc + iyh], dEx));
+                            psi_out(k, 2, m, c, ps, psy_h + (size_t)ysx * (nx + 1) + xcol[c]);
+                            ox[c] = O::fma(-O::mul(chez, dEx), cpml[3 * nc + iyh], px_[k][c]);
+                            ox[c] = O::fma(-O::mul(chez, dxr), ps, ox[c]);
+                        }
                         if (clampnan) {
                             if (dev_isnan(ox[c])) ox[c] = Real(0);
                             if (dev_isnan(oy[c])) oy[c] = Real(0);
@@ -411,14 +449,23 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, 
                     for (int c = 0; c < COLS; ++c) {
                         const int mi = (pmat[k] >> (8 * c)) & kMatMask;
                         Real Ca, Cb, Cj, Bp;
-                        load_coefs(sm.tab[wib][mi], Ca, Cb, Cj, Bp);
+                        load_coefs(ws.tab[mi], Ca, Cb, Cj, Bp);
                         const Real hyL = (c > 0) ? oy[c - 1] : hyL_first;
                         const Real dHy = O::sub(oy[c], hyL);
                         const Real dHx = O::sub(ox[c], hxn[k][c]);
                         const Real ez = pz[k][c], jp = pj[k][c];
                         Real out;
-                        if (kRef) out = O::fma(Ca, ez, O::sub(O::mul(Cb, dHy), O::mul(Cb, dHx)));
-                        else out = O::fma(Ca, ez, O::mul(Cb, O::sub(dHy, dHx)));
+                        if (kRef) {
+                            out = O::fma(Ca, ez, O::sub(O::mul(Cb, dHy), O::mul(Cb, dHx)));
+                        } else if (iye >= 0) {
+                            const int ysx = (m <= nc) ? m - 1 : m - (ny - nc) + nc;
+                            const Real qy = O::fma(cpml[nc + iye], psi_in(k, 3, m, c), O::mul(cpml[2 * nc + iye], dHx));
+                            psi_out(k, 3, m, c, qy, psy_e + (size_t)ysx * (nx + 1) + xcol[c]);
+                            const Real cy = O::mul(dHx, cpml[iye]);
+                            out = O::fma(Ca, ez, O::mul(Cb, O::fma(dxr, O::sub(Real(0), qy), O::sub(dHy, cy))));
+                        } else {
+                            out = O::fma(Ca, ez, O::mul(Cb, O::sub(dHy, dHx)));
+                        }
                         out = O::fma(-Cj, jp, out);
                         oj[c] = O::fma(Kp, jp, O::mul(Bp, O::sub(out, ez)));
                         if (clampnan && dev_isnan(out)) out = Real(0);
@@ -478,8 +525,8 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, 
                             const uint32_t mb = (pmat[k] >> (8 * c)) & 0xffu;
                             const int mi = mb & kMatMask;
                             const Real* cf = D.mtab + mi * kMatCoef;     // cold columns (global, cached)
-                            const Real Ca = sm.tab[wib][mi][kCa], Cb = sm.tab[wib][mi][kCb];
-                            const Real Cj = sm.tab[wib][mi][kCj], Bp = sm.tab[wib][mi][kBp];
+                            Real Ca, Cb, Cj, Bp;
+                            load_coefs(ws.tab[mi], Ca, Cb, Cj, Bp);
                             Real hyL = (c > 0) ? oy[c - 1] : hyL_first;
                             Real dHy = O::sub(oy[c], hyL);
                             Real dHx = O::sub(ox[c], hxn[k][c]);
@@ -581,7 +628,7 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, 
                                 if (face_slot[c] >= 0) {
                                     Real ezR2 = (c + 1 < COLS) ? oz[c + 1] : ezR2_last;
                                     Real e = O::mul(O::add(oz[c], ezR2), Real(0.5));
-                                    Real* s = sm.ring[wib][face_slot[c]][m % kRing][k];
+                                    Real* s = ws.ring[face_slot[c]][m % kRing][k];
                                     s[0] = oy[c];
                                     s[1] = e;
                                 }
@@ -668,7 +715,7 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, int strip, 
                                      c3 = a[7];
                                 for (int k = 0; k < nsteps; ++k) {
                                     const Real* p = phasor + ((size_t)(n0 + k) * nfreq + f) * 4;
-                                    const Real* sm_s = sm.ring[wib][face][m % kRing][k];
+                                    const Real* sm_s = ws.ring[face][m % kRing][k];
                                     Real h = sgn * sm_s[0], e = sgn * sm_s[1];
                                     acc_add(s0, c0, Op<Real>::mul(h, p[0]));
                                     acc_add(s1, c1, Op<Real>::mul(h, p[1]));
@@ -704,8 +751,7 @@ __global__ void __launch_bounds__(128, MINB) fdtd_advance_kernel(const SolveDesc
                                                                   const WorkItem* __restrict__ items, int nitems,
                                                                   int* __restrict__ counter) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    AdvanceSmem<Real, T, COLS>& sm = *reinterpret_cast<AdvanceSmem<Real, T, COLS>*>(smem_raw);
-    const int wib = threadIdx.x >> 5;
+    unsigned char* const wbase = smem_raw + (threadIdx.x >> 5) * warp_smem_bytes<Real, T, COLS>();
     const int lane = threadIdx.x & 31;
     for (;;) {
         int it = 0;
@@ -715,7 +761,10 @@ __global__ void __launch_bounds__(128, MINB) fdtd_advance_kernel(const SolveDesc
         const WorkItem wi = items[it];
         const SolveDesc<Real>* __restrict__ D = descs + wi.solve;
         if (!D->active) continue;
-        advance_item<Real, T, COLS, MODE>(D, wi.strip, sm, wib);
+        if (COLS > 1 && wi.narrow)
+            advance_item<Real, T, 1, MODE>(D, wi, *reinterpret_cast<WarpSmem<Real, T, 1>*>(wbase));
+        else
+            advance_item<Real, T, COLS, MODE>(D, wi, *reinterpret_cast<WarpSmem<Real, T, COLS>*>(wbase));
         __syncwarp();
     }
 }

@@ -294,7 +294,11 @@ int EngineT<Real>::serve_step(int* n_active) {
         std::vector<WorkItem> items;
         for (auto& kv : st->reqs) {
             const ServeRequest<Real>& r = *kv.second;
-            if (r.state == kRunning) append_items(items, r.first, r.nsolves, r.cd->pc.nx, st->blk.T, st->blk.cols);
+            if (r.state != kRunning) continue;
+            const size_t n0 = items.size();
+            append_items(items, r.first, r.nsolves, r.cd->pc.nx, r.cd->pc.nc, item_face_distance(r.cd->pc), st->blk.T,
+                         st->blk.cols);
+            TOMO_TRY(validate_items(items, n0, r.cd->pc.nx, st->blk.T, st->blk.cols));
         }
         st->nitems = (int)items.size();
         if (!items.empty()) {

@@ -24,6 +24,7 @@ constexpr int kMatPadLeft = 32;  // bytes of padding left of x = 0 in every mate
 constexpr int kMaxMat = 128;     // material indices per solve (7 bits)
 constexpr int kMatCoef = 8;      // coefficient columns, see MatCol
 constexpr int kMaxRx = 64;
+constexpr int kMaxCpml = 32;     // CPML cells per side (the profile lives in shared memory)
 constexpr int kRing = 64;        // rows buffered for vertical-face DFT samples
 
 enum SolveFlags : int {
