@@ -342,6 +342,66 @@ def run_ours(args) -> None:
         dist.destroy_process_group()
 
 
+def run_large(args) -> None:
+    """Large-batch workload: 2048x2048 grid, dx 0.125 mm, 16-cell CPML, 20000
+    steps, 32 transmitters per candidate, 16 ellipses in a skin-layer disc, NTFF
+    at 16 frequencies over 720 angles.  The full 64-candidate batch holds about
+    400 GB of state; this times a bounded subset of candidates (all their
+    transmitters, full steps) and compares FP32 with the FP64 GPU path on the
+    first transmitters of one candidate."""
+    rank, world, _ = _rank_info()
+    if rank != 0:
+        return
+    import torch
+
+    torch.cuda.set_device(0)
+    import tomography_gb300 as T
+    from tomography_gb300 import workloads as W
+
+    spec = T.breast_spec(4)
+    if args.large_steps:
+        spec = spec.copy(steps=args.large_steps)
+    K = spec.n_ellipses
+    ncand = args.large_candidates
+    cands = W.candidate_batch(4, ncand, K, disc_radius=spec.disc_radius)
+    with T.Solver(spec) as s:
+        # the autotuner and the graph build run before the timed time loop (advance_ms)
+        sampler = ClockSampler(0)
+        sampler.start()
+        out = s.forward(cands, traces=False, far_field=True)
+        clocks = sampler.stop()
+        st = s.stats()
+    gcells = st["cell_updates"] / (st["advance_ms"] * 1e6)
+    # FP32 vs FP64 GPU on the first transmitters of candidate 0
+    ntx = args.large_check_tx
+    sub = spec.copy(n_tx=ntx)
+    res = {}
+    for name, prec in (("fp32", T.FP32), ("fp64", T.FP64)):
+        with T.Solver(sub.copy(precision=prec)) as s:
+            res[name] = s.forward(cands[:1], traces=True, traces_f64=True, far_field=True)
+    t32, t64 = res["fp32"]["traces_f64"][0], res["fp64"]["traces_f64"][0]
+    d32, d64 = res["fp32"]["D"][0].astype(np.float64), res["fp64"]["D"][0].astype(np.float64)
+    line = {
+        "metric": "Gcell-updates/s", "value": gcells, "unit": "Gcell-updates/s", "n_gpus": 1, "steps": 1,
+        "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded candidates)",
+        "config": {"workload": "large batch: 2048x2048, dx 0.125 mm, 16-cell CPML, %d steps, 32 tx/candidate, "
+                               "16 ellipses, NTFF 16 freqs x 720 angles" % spec.steps,
+                   "candidates": ncand, "solves": ncand * spec.n_tx,
+                   "sample": "%d of the 64 candidates (the full batch needs about 400 GB of state)" % ncand,
+                   "steps_per_launch": st["steps_per_launch"], "cols_per_lane": st["cols_per_lane"],
+                   "min_blocks_per_sm": st.get("min_blocks_per_sm")},
+        "advance_s": st["advance_ms"] / 1e3, "total_s": st["total_ms"] / 1e3,
+        "algorithmic_gbs": BYTES_PER_CELL_UPDATE * gcells, "roofline_frac": BYTES_PER_CELL_UPDATE * gcells /
+        _peaks()["hbm_gbs"],
+        "error_vs_fp64_gpu": {"trace_rel_l2": float(np.linalg.norm(t32 - t64) / np.linalg.norm(t64)),
+                              "far_field_rel_l2": float(np.linalg.norm(d32 - d64) / np.linalg.norm(d64)),
+                              "subset": "candidate 0, transmitters 0..%d" % (ntx - 1)},
+        "fitness_head": None, "D_checksum": float(np.abs(out["D"]).sum()), "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
 SERVING_EDGES = (128, 256, 512, 1024)
 SERVING_ANTENNAS = (8, 16, 24, 32)
 
@@ -450,7 +510,10 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--candidates", type=int, default=N_CAND)
     ap.add_argument("--no-extras", action="store_true")
-    ap.add_argument("--workload", default="pso", choices=["pso", "serving"])
+    ap.add_argument("--workload", default="pso", choices=["pso", "serving", "large"])
+    ap.add_argument("--large-steps", type=int, default=0, help="large: override the 20000 steps")
+    ap.add_argument("--large-candidates", type=int, default=2, help="large: candidates timed")
+    ap.add_argument("--large-check-tx", type=int, default=2, help="large: transmitters compared with FP64")
     ap.add_argument("--requests", type=int, default=40, help="serving: requests in the sample")
     ap.add_argument("--batch-min", type=int, default=2, help="serving: smallest candidate batch")
     ap.add_argument("--batch-max", type=int, default=16, help="serving: largest candidate batch")
@@ -460,6 +523,8 @@ def main() -> None:
     args = ap.parse_args()
     if args.workload == "serving" and args.impl == "ours":
         run_serving(args)
+    elif args.workload == "large" and args.impl == "ours":
+        run_large(args)
     elif args.impl == "reference":
         run_reference(args)
     else:
