@@ -194,6 +194,7 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
     constexpr int P = 32 * COLS;
     static_assert(P > 2 * T, "a strip must own at least one column");
     constexpr bool kRef = MODE == kModeRef;
+    constexpr bool kEdgePath = !kRef && COLS == 1;   // edge strips use the narrow layout
     const int lane = threadIdx.x & 31;
     const int nx = D.nx, ny = D.ny, nc = D.ncpml, S = D.steps_total, n0 = D.step;
     const int nsteps = min(T, S - n0);
@@ -470,6 +471,99 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
                         oj[c] = O::fma(Kp, jp, O::mul(Bp, O::sub(out, ez)));
                         if (clampnan && dev_isnan(out)) out = Real(0);
                         oz[c] = out;
+                    }
+                } else if (kEdgePath && k < nsteps && !rowbit) {
+                    // ================= edge path (breast mode, narrow strips at the left
+                    // and right edges): the fast path's straight-line code with the
+                    // x-CPML terms computed branch-free on every lane and chosen per lane
+                    // by select, row-uniform y-CPML terms, and the PEC boundary and the
+                    // padding columns held by select.  Each value is chosen from the same
+                    // explicitly rounded formulas the general path evaluates, so every
+                    // cell gets the same bits.  (Values computed for lanes that do not
+                    // select them may come from stale shared memory; they are discarded.)
+                    const int iyh = (m < nc) ? nc - 1 - m : ((m >= ny - nc) ? m - ny + nc : -1);
+                    const int iye = (m <= nc) ? nc - m : ((m >= ny - nc) ? m - ny + nc : -1);
+                    const Real ezR_last = __shfl_down_sync(0xffffffffu, pz[k][0], 1);
+#pragma unroll
+                    for (int c = 0; c < COLS; ++c) {
+                        const int x = xcol[c];
+                        const bool hin = x >= 0 && x < nx;
+                        const bool isx = ixh[c] >= 0;
+                        const int i = isx ? ixh[c] : 0;
+                        const Real ez0 = pz[k][c];
+                        const Real ezR = (c + 1 < COLS) ? pz[k][c + 1] : ezR_last;
+                        const Real hx0 = px_[k][c], hy0 = py_[k][c];
+                        const Real dEy = O::sub(ezR, ez0);
+                        const Real dEx = O::sub(iz[c], ez0);
+                        Real hy = O::fma(chez, dEy, hy0);
+                        Real hx = O::fma(-chez, dEx, hx0);
+                        const Real psx = O::fma(cpml[4 * nc + i], psi_in(k, 0, m, c), O::mul(cpml[5 * nc + i], dEy));
+                        Real hyc = O::fma(O::mul(chez, dEy), cpml[3 * nc + i], hy0);
+                        hyc = O::fma(O::mul(chez, dxr), psx, hyc);
+                        if (isx) {
+                            const int xsx = (x < nc) ? x : x - (nx - nc) + nc;
+                            psi_out(k, 0, m, c, psx, psx_h + (size_t)m * 2 * nc + xsx);
+                        }
+                        hy = isx ? hyc : hy;
+                        if (iyh >= 0) {
+                            const int ysx = (m < nc) ? m : m - (ny - nc) + nc;
+                            const Real ps = O::fma(cpml[4 * nc + iyh], psi_in(k, 2, m, c), O::mul(cpml[5 * nc + iyh], dEx));
+                            if (hin) psi_out(k, 2, m, c, ps, psy_h + (size_t)ysx * (nx + 1) + x);
+                            hx = O::fma(-O::mul(chez, dEx), cpml[3 * nc + iyh], hx0);
+                            hx = O::fma(-O::mul(chez, dxr), ps, hx);
+                        }
+                        ox[c] = hin ? hx : hx0;
+                        oy[c] = hin ? hy : hy0;
+                    }
+                    const Real hyL_first = __shfl_up_sync(0xffffffffu, oy[COLS - 1], 1);
+#pragma unroll
+                    for (int c = 0; c < COLS; ++c) {
+                        const int x = xcol[c];
+                        const bool ein = x >= 1 && x <= nx - 1;
+                        const bool isx = ixe[c] >= 0;
+                        const int i = isx ? ixe[c] : 0;
+                        const int mi = (pmat[k] >> (8 * c)) & kMatMask;
+                        Real Ca, Cb, Cj, Bp;
+                        load_coefs(ws.tab[mi], Ca, Cb, Cj, Bp);
+                        const Real hyL = (c > 0) ? oy[c - 1] : hyL_first;
+                        const Real dHy = O::sub(oy[c], hyL);
+                        const Real dHx = O::sub(ox[c], hxn[k][c]);
+                        const Real ez = pz[k][c], jp = pj[k][c];
+                        const Real qxc = O::fma(cpml[nc + i], psi_in(k, 1, m, c), O::mul(cpml[2 * nc + i], dHy));
+                        if (isx) {
+                            const int xsx = (x <= nc) ? x - 1 : x - (nx - nc) + nc;
+                            psi_out(k, 1, m, c, qxc, psx_e + (size_t)m * 2 * nc + xsx);
+                        }
+                        const Real cxc = O::mul(dHy, cpml[i]);
+                        const Real qx = isx ? qxc : Real(0);
+                        const Real cx = isx ? cxc : dHy;
+                        Real qy = Real(0), cy = dHx;
+                        if (iye >= 0) {
+                            const int ysx = (m <= nc) ? m - 1 : m - (ny - nc) + nc;
+                            qy = O::fma(cpml[nc + iye], psi_in(k, 3, m, c), O::mul(cpml[2 * nc + iye], dHx));
+                            if (ein) psi_out(k, 3, m, c, qy, psy_e + (size_t)ysx * (nx + 1) + x);
+                            cy = O::mul(dHx, cpml[iye]);
+                        }
+                        const Real outc = O::fma(Ca, ez, O::mul(Cb, O::fma(dxr, O::sub(qx, qy), O::sub(cx, cy))));
+                        const Real outp = O::fma(Ca, ez, O::mul(Cb, O::sub(dHy, dHx)));
+                        Real out = (isx || iye >= 0) ? outc : outp;
+                        out = O::fma(-Cj, jp, out);
+                        const Real jpo = O::fma(Kp, jp, O::mul(Bp, O::sub(out, ez)));
+                        oz[c] = ein ? out : Real(0);
+                        oj[c] = ein ? jpo : jp;
+                    }
+                    // vertical NTFF faces: buffer (h, e) samples for the warp-wide flush
+                    if (nfreq > 0 && (has_face0 || has_face1) && m >= fd && m <= ny - fd - 1) {
+                        const Real ezR2_last = __shfl_down_sync(0xffffffffu, oz[0], 1);
+#pragma unroll
+                        for (int c = 0; c < COLS; ++c) {
+                            if (face_slot[c] >= 0) {
+                                const Real ezR2 = (c + 1 < COLS) ? oz[c + 1] : ezR2_last;
+                                Real* smp = ws.ring[face_slot[c]][m % kRing][k];
+                                smp[0] = oy[c];
+                                smp[1] = O::mul(O::add(oz[c], ezR2), Real(0.5));
+                            }
+                        }
                     }
                 } else if (k < nsteps) {
                     // ================= general path
