@@ -67,6 +67,25 @@ def test_blocking_depths_bit_identical(tomo, T_cols):
     np.testing.assert_array_equal(out["D"], ref["D"])
 
 
+@pytest.mark.parametrize("T_cols", [(2, 1), (2, 2), (4, 1), (4, 2)])
+def test_wide_and_narrow_items_bit_identical(tomo, T_cols):
+    """A 200x200 grid, where COLS = 2 blockings split each solve into narrow
+    edge strips and wide interior strips (the 96x96 grid above is narrow
+    throughout): the same bits as one step per launch, one column per lane."""
+    from tomography_gb300 import workloads as W
+
+    T, cols = T_cols
+    base = tomo.breast_spec(0).copy(steps=301, n_tx=2)
+    params = W.phantom_params(W.config_seed(0) + 3, base.n_ellipses)
+    with tomo.Solver(base.copy(steps_per_launch=1, cols_per_lane=1)) as s:
+        ref = s.forward(params, traces=True, far_field=True)
+    with tomo.Solver(base.copy(steps_per_launch=T, cols_per_lane=cols)) as s:
+        out = s.forward(params, traces=True, far_field=True)
+    np.testing.assert_array_equal(out["traces"], ref["traces"])
+    np.testing.assert_array_equal(out["D"], ref["D"])
+    assert np.abs(ref["traces"]).max() > 0
+
+
 def test_fitness_fp32_vs_oracle(tomo, oracle):
     from tomography_gb300 import workloads as W
 

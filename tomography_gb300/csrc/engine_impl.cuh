@@ -322,7 +322,7 @@ int advance_grid(const Blocking& b, int mode, int nitems, int num_sms, int* bloc
 // first batch is tuned.
 template <typename Real>
 std::vector<Blocking> tune_candidates(int mode, int fixT, int fixCols, int fixMinb) {
-    static const int pref[][3] = {{2, 2, 2}, {2, 1, 3}, {2, 2, 3}, {2, 1, 2}, {2, 1, 4}, {4, 1, 2}, {4, 1, 3},
+    static const int pref[][3] = {{2, 2, 3}, {2, 2, 2}, {2, 1, 3}, {2, 1, 2}, {2, 1, 4}, {4, 1, 2}, {4, 1, 3},
                                   {4, 2, 2}, {1, 1, 2}, {1, 1, 4}, {6, 1, 2}, {8, 1, 2}};
     std::vector<Blocking> out;
     for (const auto& p : pref) {
@@ -365,18 +365,33 @@ inline void append_items(std::vector<WorkItem>& items, int first, int nsolves, i
     // Wide items copy rows COLS elements at a time, so their column windows
     // start at multiples of COLS: every wide-item boundary is = T (mod COLS)
     // (the window of a full item starts at x0 - T, a clipped one at x1 + T - P).
-    const int a = (lo + 1 + T + W1 - 1) / W1 * W1;          // first interior column: a - T > lo
-    int b = ncol - (ncol - hi + T + W1 - 1) / W1 * W1;        // interior end: b - 1 + T < hi
-    b -= (((b - T) % cols) + cols) % cols;
-    const bool aligned = cols == 1 || ((a - T) % cols == 0 && (2 * T) % cols == 0);
-    if (cols == 1 || !aligned || b - a < W2) {
+    int a_min = lo + 1 + T;                                   // first interior column: a - T > lo
+    a_min += (((T - a_min) % cols) + cols) % cols;
+    int b_max = hi - T;                                       // interior end: b - 1 + T < hi
+    b_max -= (((b_max - T) % cols) + cols) % cols;
+    // Interior bounds: fewest items, then fewest narrow columns (the narrow
+    // edge strips take the slack the wide strips would otherwise leave).
+    int a = a_min, b = b_max;
+    long best = -1;
+    for (int aa = a_min; aa <= a_min + W1; aa += cols)
+        for (int bb = b_max; bb >= b_max - W1 && bb - aa >= W2; bb -= cols) {
+            const long n = (aa + W1 - 1) / W1 + (ncol - bb + W1 - 1) / W1 + (bb - aa + W2 - 1) / W2;
+            const long key = n * 100000L + aa + (ncol - bb);
+            if (best < 0 || key < best) {
+                best = key;
+                a = aa;
+                b = bb;
+            }
+        }
+    const bool aligned = cols == 1 || (2 * T) % cols == 0;   // then every wide boundary stays = T
+    if (cols == 1 || !aligned || best < 0) {
         const int n = (ncol + W1 - 1) / W1;
         for (int q = 0; q < n; ++q) {
             const WorkItem w{0, q * W1, std::min((q + 1) * W1, ncol), cols > 1 ? 1 : 0};
             (q == 0 || q == n - 1 ? edge : mid).push_back(w);
         }
     } else {
-        for (int x = 0; x < a; x += W1) edge.push_back({0, x, x + W1, 1});
+        for (int x = 0; x < a; x += W1) edge.push_back({0, x, std::min(x + W1, a), 1});
         for (int x = b; x < ncol; x += W1) edge.push_back({0, x, std::min(x + W1, ncol), 1});
         for (int x = a; x < b; x += W2) mid.push_back({0, x, std::min(x + W2, b), 0});
     }
