@@ -7,9 +7,9 @@
 //     n_exc solves; a request may carry its own grid spec);
 //   * tomo_serve_step admits queued requests in FIFO order while their memory
 //     fits the HBM budget and descriptor slots are free, then advances EVERY
-//     admitted solve by one launch of the descriptor-driven advance kernel
-//     (solves of different requests, grid sizes and progress share the
-//     launch), and retires requests whose solves reached their last step
+//     admitted solve by up to four launches of the descriptor-driven advance
+//     kernel (solves of different requests, grid sizes and progress share
+//     the launches), and retires requests whose solves reached their last step
 //     (far field + misfit on the device, fitness to the host);
 //   * tomo_poll returns a finished request's fitness.
 // Each solve's arithmetic depends only on its own descriptor, so a result is
@@ -312,17 +312,29 @@ int EngineT<Real>::serve_step(int* n_active) {
         CUDA_TRY(cudaStreamSynchronize(stream_));
         st->items_dirty = false;
     }
-    // 3. one advance launch over everything admitted
+    // 3. advance launches over everything admitted: as many as the running
+    // request closest to its end still needs, at most kLaunchesPerStep, so
+    // that no request runs past its last step and the host synchronises once
+    // per serving step rather than once per launch
+    constexpr int kLaunchesPerStep = 4;
     int running = 0;
     if (st->nitems > 0) {
-        launch_advance<Real>(st->blk, advance_mode(cd_.pc.spec), st->blocks, st->smem,
-                             st->descs.template as<SolveDesc<Real>>(), st->items.template as<WorkItem>(), st->nitems,
-                             st->hi_slot, d_counter_.as<int>(), stream_);
+        int nl = kLaunchesPerStep;
+        for (auto& kv : st->reqs) {
+            const ServeRequest<Real>& r = *kv.second;
+            if (r.state == kRunning)
+                nl = std::min(nl, (r.cd->pc.S - r.steps_done + st->blk.T - 1) / st->blk.T);
+        }
+        nl = std::max(nl, 1);
+        for (int l = 0; l < nl; ++l)
+            launch_advance<Real>(st->blk, advance_mode(cd_.pc.spec), st->blocks, st->smem,
+                                 st->descs.template as<SolveDesc<Real>>(), st->items.template as<WorkItem>(),
+                                 st->nitems, st->hi_slot, d_counter_.as<int>(), stream_);
         CUDA_TRY(cudaGetLastError());
         for (auto& kv : st->reqs) {
             ServeRequest<Real>& r = *kv.second;
             if (r.state != kRunning) continue;
-            r.steps_done += st->blk.T;
+            r.steps_done += nl * st->blk.T;
             if (r.steps_done >= r.cd->pc.S) TOMO_TRY(retire(st, r, stream_, true));
             else ++running;
         }
