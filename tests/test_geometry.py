@@ -15,11 +15,11 @@ import pytest
 PAD_LEFT, PAD_RIGHT = 32, 160
 
 
-def _items(lib, nx, nc, d, T, cols):
-    buf = (C.c_int * 3000)()
-    n = lib.tomo_internal_work_items(nx, nc, d, T, cols, buf, 1000)
+def _items(lib, nx, nc, d, T, cols, ny=None, nseg=1):
+    buf = (C.c_int * 50000)()
+    n = lib.tomo_internal_work_items(nx, nx if ny is None else ny, nc, d, T, cols, nseg, buf, 10000)
     assert n > 0, lib.tomo_last_error()
-    return [(buf[3 * i], buf[3 * i + 1], buf[3 * i + 2]) for i in range(n)]
+    return [tuple(buf[5 * i + j] for j in range(5)) for i in range(n)]
 
 
 @pytest.mark.parametrize("T,cols", [(1, 1), (2, 1), (2, 2), (3, 1), (3, 2), (4, 1), (4, 2), (6, 1), (8, 1)])
@@ -35,7 +35,8 @@ def test_strip_geometry(tomo, T, cols):
                 if d >= 0 and 2 * d + 4 > nx:
                     continue
                 owned = [0] * (nx + 1)
-                for x0, x1, narrow in _items(lib, nx, nc, d, T, cols):
+                for x0, x1, narrow, y0, y1 in _items(lib, nx, nc, d, T, cols):
+                    assert (y0, y1) == (0, nx + 1)
                     c = cols if (cols > 1 and not narrow) else 1
                     P = 32 * c
                     xs = x1 + T - P
@@ -52,3 +53,16 @@ def test_strip_geometry(tomo, T, cols):
                 assert owned == [1] * (nx + 1), (nx, nc, d)
     if cols > 1:
         assert wide_seen > 0
+
+
+@pytest.mark.parametrize("nseg", [2, 3, 7])
+def test_row_segments_cover_every_cell_once(tomo, nseg):
+    lib = tomo.library()
+    for nx, ny, nc, d in ((96, 96, 8, 11), (200, 150, 10, 13), (400, 400, 12, 15)):
+        cover = [[0] * (ny + 1) for _ in range(nx + 1)]
+        for x0, x1, _, y0, y1 in _items(lib, nx, nc, d, 2, 2, ny=ny, nseg=nseg):
+            assert 0 <= y0 < y1 <= ny + 1
+            for x in range(x0, x1):
+                for y in range(y0, y1):
+                    cover[x][y] += 1
+        assert all(v == 1 for col in cover for v in col), (nx, ny, nseg)

@@ -86,6 +86,25 @@ def test_wide_and_narrow_items_bit_identical(tomo, T_cols):
     assert np.abs(ref["traces"]).max() > 0
 
 
+@pytest.mark.parametrize("nseg", [5, 13])
+def test_row_segments_bit_identical(tomo, nseg, monkeypatch):
+    """Strips cut into row segments (used when a batch is too small to fill
+    the GPU; each segment recomputes 2T halo rows) give the same bits as whole
+    strips: fields, receiver traces and far field."""
+    from tomography_gb300 import workloads as W
+
+    spec = tomo.breast_spec(0).copy(steps=301, n_tx=2, steps_per_launch=2, cols_per_lane=2)
+    params = W.phantom_params(W.config_seed(0) + 5, spec.n_ellipses)
+    monkeypatch.setenv("TOMO_SEGMENTS", "1")
+    with tomo.Solver(spec) as s:
+        ref = s.forward(params, traces=True, far_field=True)
+    monkeypatch.setenv("TOMO_SEGMENTS", str(nseg))
+    with tomo.Solver(spec) as s:
+        out = s.forward(params, traces=True, far_field=True)
+    np.testing.assert_array_equal(out["traces"], ref["traces"])
+    np.testing.assert_array_equal(out["D"], ref["D"])
+
+
 def test_fitness_fp32_vs_oracle(tomo, oracle):
     from tomography_gb300 import workloads as W
 

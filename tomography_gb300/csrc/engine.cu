@@ -514,8 +514,11 @@ int EngineT<Real>::autotune(size_t ncand) {
     std::vector<WorkItem> items;
     for (const Blocking& c : cands) {
         items.clear();
-        append_items(items, 0, nsolves, pc.nx, pc.nc, item_face_distance(pc), c.T, c.cols);
-        TOMO_TRY(validate_items(items, 0, pc.nx, c.T, c.cols));
+        const int nseg = choose_segments(
+            (long)nsolves * items_per_solve(pc.nx, pc.ny, pc.nc, item_face_distance(pc), c.T, c.cols), pc.ny, c.T,
+            24L * num_sms_);
+        append_items(items, 0, nsolves, pc.nx, pc.ny, pc.nc, item_face_distance(pc), c.T, c.cols, nseg);
+        TOMO_TRY(validate_items(items, 0, pc.nx, pc.ny, c.T, c.cols));
         TOMO_TRY(d_tune_items_.ensure(sizeof(WorkItem) * items.size()));
         CUDA_TRY(cudaMemcpyAsync(d_tune_items_.p, items.data(), sizeof(WorkItem) * items.size(), cudaMemcpyHostToDevice,
                                  stream_));
@@ -597,8 +600,11 @@ int EngineT<Real>::ensure_batch(int ncand) {
         cap_cand_ = ncand;
     }
     std::vector<WorkItem> items;
-    append_items(items, 0, nsolves, pc.nx, pc.nc, item_face_distance(pc), blk_.T, blk_.cols);
-    TOMO_TRY(validate_items(items, 0, pc.nx, blk_.T, blk_.cols));
+    const int nseg = choose_segments(
+        (long)nsolves * items_per_solve(pc.nx, pc.ny, pc.nc, item_face_distance(pc), blk_.T, blk_.cols), pc.ny,
+        blk_.T, 24L * num_sms_);
+    append_items(items, 0, nsolves, pc.nx, pc.ny, pc.nc, item_face_distance(pc), blk_.T, blk_.cols, nseg);
+    TOMO_TRY(validate_items(items, 0, pc.nx, pc.ny, blk_.T, blk_.cols));
     if (nsolves != nsolves_ || (int)items.size() != nitems_ || ncand != cur_cand_ || blk_.T != items_blk_.T ||
         blk_.cols != items_blk_.cols) {
         invalidate_graph();
@@ -785,17 +791,19 @@ int create_engine(const tomo_spec* spec, EngineBase** out) {
 }  // namespace tomo
 
 // Internal test hook (not part of the public ABI): the work items the engine
-// launches for one solve of a grid, as (x0, x1, narrow) triples, after the
-// same host validation.  Returns the item count, or a negative status.
-extern "C" int tomo_internal_work_items(int nx, int ncpml, int d, int T, int cols, int* out, int cap) {
+// launches for one solve of an nx x ny grid cut into nseg row segments, as
+// (x0, x1, narrow, y0, y1) records, after the same host validation.  Returns
+// the item count, or a negative status.
+extern "C" int tomo_internal_work_items(int nx, int ny, int ncpml, int d, int T, int cols, int nseg, int* out,
+                                        int cap) {
     std::vector<tomo::WorkItem> items;
-    tomo::append_items(items, 0, 1, nx, ncpml, d, T, cols);
-    TOMO_TRY(tomo::validate_items(items, 0, nx, T, cols));
+    tomo::append_items(items, 0, 1, nx, ny, ncpml, d, T, cols, nseg);
+    TOMO_TRY(tomo::validate_items(items, 0, nx, ny, T, cols));
     if (!out || (int)items.size() > cap) return tomo::fail(TOMO_EINVAL, "item buffer too small");
     for (size_t i = 0; i < items.size(); ++i) {
-        out[3 * i] = items[i].x0;
-        out[3 * i + 1] = items[i].x1;
-        out[3 * i + 2] = items[i].narrow;
+        const tomo::WorkItem& w = items[i];
+        const int rec[5] = {w.x0, w.x1, w.narrow, w.y0, w.y1};
+        for (int j = 0; j < 5; ++j) out[5 * i + j] = rec[j];
     }
     return (int)items.size();
 }

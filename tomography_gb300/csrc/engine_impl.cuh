@@ -4,8 +4,10 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <string>
@@ -355,8 +357,8 @@ void launch_advance(const Blocking& b, int mode, int blocks, size_t smem, const 
 // would reach into them, go to narrow items (32 - 2T owned columns) and the
 // rest to wide items (32*COLS - 2T), so the general path runs on as few lanes
 // as possible.  The edge items of every solve come first: they cost the most.
-inline void append_items(std::vector<WorkItem>& items, int first, int nsolves, int nx, int ncpml, int d, int T,
-                         int cols) {
+inline void append_items(std::vector<WorkItem>& items, int first, int nsolves, int nx, int ny, int ncpml, int d, int T,
+                         int cols, int nseg = 1) {
     const int W1 = 32 - 2 * T, W2 = 32 * cols - 2 * T;
     const int ncol = nx + 1;
     std::vector<WorkItem> edge, mid;   // one solve's items (solve index filled in below)
@@ -387,38 +389,58 @@ inline void append_items(std::vector<WorkItem>& items, int first, int nsolves, i
     if (cols == 1 || !aligned || best < 0) {
         const int n = (ncol + W1 - 1) / W1;
         for (int q = 0; q < n; ++q) {
-            const WorkItem w{0, q * W1, std::min((q + 1) * W1, ncol), cols > 1 ? 1 : 0};
+            const WorkItem w{0, q * W1, std::min((q + 1) * W1, ncol), cols > 1 ? 1 : 0, 0, ny + 1};
             (q == 0 || q == n - 1 ? edge : mid).push_back(w);
         }
     } else {
-        for (int x = 0; x < a; x += W1) edge.push_back({0, x, std::min(x + W1, a), 1});
-        for (int x = b; x < ncol; x += W1) edge.push_back({0, x, std::min(x + W1, ncol), 1});
-        for (int x = a; x < b; x += W2) mid.push_back({0, x, std::min(x + W2, b), 0});
+        for (int x = 0; x < a; x += W1) edge.push_back({0, x, std::min(x + W1, a), 1, 0, ny + 1});
+        for (int x = b; x < ncol; x += W1) edge.push_back({0, x, std::min(x + W1, ncol), 1, 0, ny + 1});
+        for (int x = a; x < b; x += W2) mid.push_back({0, x, std::min(x + W2, b), 0, 0, ny + 1});
     }
-    for (int sv = 0; sv < nsolves; ++sv)
-        for (WorkItem w : edge) {
-            w.solve = first + sv;
-            items.push_back(w);
-        }
-    for (int sv = 0; sv < nsolves; ++sv)
-        for (WorkItem w : mid) {
-            w.solve = first + sv;
-            items.push_back(w);
-        }
+    // row segments: [0, ny] cut into nseg nearly equal ranges
+    const int nrow = ny + 1;
+    nseg = std::max(1, std::min(nseg, nrow));
+    for (const std::vector<WorkItem>* list : {&edge, &mid})
+        for (int sv = 0; sv < nsolves; ++sv)
+            for (WorkItem w : *list)
+                for (int g = 0; g < nseg; ++g) {
+                    w.solve = first + sv;
+                    w.y0 = (int)((long)nrow * g / nseg);
+                    w.y1 = (int)((long)nrow * (g + 1) / nseg);
+                    items.push_back(w);
+                }
+}
+
+// Work items of one solve before row segmentation.
+inline int items_per_solve(int nx, int ny, int ncpml, int d, int T, int cols) {
+    std::vector<WorkItem> v;
+    append_items(v, 0, 1, nx, ny, ncpml, d, T, cols, 1);
+    return (int)v.size();
+}
+
+// Row segments per strip: 1 while a batch's strips fill the GPU, else enough
+// to reach about min_items items, keeping segments at least 8T and 32 rows
+// tall (each segment recomputes 2T halo rows).  TOMO_SEGMENTS fixes the count.
+inline int choose_segments(long strips, int ny, int T, long min_items) {
+    if (const char* e = std::getenv("TOMO_SEGMENTS")) return std::max(1, std::atoi(e));
+    if (strips <= 0 || strips >= min_items) return 1;
+    const int max_seg = std::max(1, (ny + 1) / std::max(32, 8 * T));
+    return (int)std::max(1L, std::min<long>(max_seg, (min_items + strips - 1) / strips));
 }
 
 // Host check of work items before they reach the GPU: owned ranges inside the
 // grid and no wider than the layout allows, column windows inside the zero
 // padding of the field rows, and wide windows aligned for COLS-element copies.
 // A violation is a geometry bug; it fails the call instead of launching.
-inline int validate_items(const std::vector<WorkItem>& items, size_t first_item, int nx, int T, int cols) {
+inline int validate_items(const std::vector<WorkItem>& items, size_t first_item, int nx, int ny, int T, int cols) {
     for (size_t i = first_item; i < items.size(); ++i) {
         const WorkItem& w = items[i];
         const int c = (cols > 1 && !w.narrow) ? cols : 1;
         const int P = 32 * c;
         const int xs = w.x1 + T - P;
         if (w.x0 < 0 || w.x1 > nx + 1 || w.x1 <= w.x0 || w.x1 - w.x0 > P - 2 * T || xs > w.x0 - T ||
-            xs < -kPadLeft || xs + P > nx + 1 + kPadRight || (xs % c) != 0)
+            xs < -kPadLeft || xs + P > nx + 1 + kPadRight || (xs % c) != 0 || w.y0 < 0 || w.y1 > ny + 1 ||
+            w.y1 <= w.y0)
             return fail(TOMO_ECUDA, "internal error: work item (" + std::to_string(w.x0) + ", " + std::to_string(w.x1) +
                                         ") invalid for nx " + std::to_string(nx));
     }

@@ -43,10 +43,16 @@ namespace tomo {
 // boundary and vertical NTFF-face columns near the left and right edges, where
 // the general path runs on every row; wide items (the kernel's COLS) cover the
 // interior, whose halo stays clear of those columns.
+//
+// A strip may be cut into row segments (owned rows [y0, y1)) when a batch has
+// too few strips to fill the GPU.  A segment's sweep starts 2T rows below y0
+// and runs until every level has advanced row y1, recomputing those halo rows;
+// only owned rows are written (fields, CPML psi, receiver samples, NTFF sums).
 struct WorkItem {
     int solve;
     int x0, x1;
     int narrow;
+    int y0, y1;
 };
 
 enum AdvanceMode : int {
@@ -205,6 +211,7 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
     // its columns never reach further right than a full strip ending at x1.
     const int xs = wi.x1 + T - P;      // column of position 0
     const int ox0 = wi.x0, ox1 = wi.x1;
+    const int y0 = wi.y0, y1 = wi.y1;   // owned rows
     const int src = D.parity, dst = 1 - src;
     const Real chez = D.chez, Kp = D.Kp, dxr = D.dx;
     const bool clampnan = kRef && (D.flags & kNanClamp) != 0;
@@ -320,7 +327,7 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
     };
     auto psi_out = [&](int k, int f, int m, int c, Real v, size_t goff) {
         if (k + 1 < T) ws.pslev[k % (T > 1 ? T - 1 : 1)][f][m & 3][lane * COLS + c] = v;
-        else if (owned[c]) psi_dst[goff] = v;
+        else if (owned[c] && m >= y0 && m < y1) psi_dst[goff] = v;
     };
     bool wxs = false;   // warp holds an x-strip column (uniform)
 #pragma unroll
@@ -378,12 +385,13 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
         }
         cp_async_commit();
     };
+    const int rstart = max(0, y0 - 2 * T);          // halo rows below the segment
+    const int rmax = min(ny, y1) + 2 * T - 1;         // every level advances row y1 (or ny)
 #pragma unroll 1
-    for (int r = 0; r < kPrefetch; ++r) issue_row(r);
+    for (int r = rstart; r < rstart + kPrefetch; ++r) issue_row(r);
 
-    const int rmax = ny + 2 * T - 1;
-    int flushed = 0;   // next face row not yet flushed
-    for (int r = 0; r <= rmax; ++r) {
+    int flushed = y0;   // next face row not yet flushed
+    for (int r = rstart; r <= rmax; ++r) {
         // ---- level 0 input: row r from the ring; request row r + kPrefetch
         cp_async_wait<kPrefetch - 1>();
         __syncwarp();
@@ -687,7 +695,7 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
                             }
                             if (clampnan && dev_isnan(out)) out = Real(0);
                             // receivers (owned cells only, so each sample is written once)
-                            if ((mb & kMatRx) && owned[c]) {
+                            if ((mb & kMatRx) && owned[c] && m >= y0 && m < y1) {
                                 for (int rr = 0; rr < D.nrx; ++rr)
                                     if (D.rx[2 * rr] == x && D.rx[2 * rr + 1] == m)
                                         D.traces[(size_t)rr * S + n] = out;
@@ -700,7 +708,7 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
                     if (nfreq > 0) {
                         const Real* ph = phasor + (size_t)n * nfreq * 4;
                         // horizontal faces: face row m-1 is complete at this level
-                        if (m - 1 == fd || m - 1 == ny - fd - 1) {
+                        if ((m - 1 == fd || m - 1 == ny - fd - 1) && m - 1 >= y0 && m - 1 < y1) {
                             const bool yp = (m - 1 == ny - fd - 1);
 #pragma unroll
                             for (int c = 0; c < COLS; ++c) {
@@ -766,7 +774,7 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
                     for (int c = 0; c < COLS; ++c) {
                         hz[k + 1][c] = oz[c]; hxr[k + 1][c] = ox[c]; hyr[k + 1][c] = oy[c]; hj[k + 1][c] = oj[c];
                     }
-                } else {
+                } else if (m >= y0 && m < y1) {   // owned rows only
                     const long long rowoff = (long long)m * pitch;
                     const bool jrow = m >= jy0 && m <= jy1;
 #pragma unroll
@@ -795,7 +803,7 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
             const bool last = (r == rmax);
             if (last || ((done + 1 - flushed) >= 32)) {
                 __syncwarp();
-                const int upto = last ? ny : done;
+                const int upto = min(last ? ny : done, y1 - 1);
                 while (flushed <= upto) {
                     const int m = flushed + lane;
                     if (m <= upto && m >= fd && m <= ny - fd - 1) {

@@ -292,13 +292,25 @@ int EngineT<Real>::serve_step(int* n_active) {
     // 2. work items of every running solve
     if (st->items_dirty) {
         std::vector<WorkItem> items;
+        long strips = 0;
+        int nymax = 0;
+        for (auto& kv : st->reqs) {
+            const ServeRequest<Real>& r = *kv.second;
+            if (r.state != kRunning) continue;
+            const ProblemClass& pc = r.cd->pc;
+            strips += (long)r.nsolves * items_per_solve(pc.nx, pc.ny, pc.nc, item_face_distance(pc), st->blk.T,
+                                                       st->blk.cols);
+            nymax = std::max(nymax, pc.ny);
+        }
+        const int nseg = choose_segments(strips, nymax, st->blk.T, 24L * num_sms_);
         for (auto& kv : st->reqs) {
             const ServeRequest<Real>& r = *kv.second;
             if (r.state != kRunning) continue;
             const size_t n0 = items.size();
-            append_items(items, r.first, r.nsolves, r.cd->pc.nx, r.cd->pc.nc, item_face_distance(r.cd->pc), st->blk.T,
-                         st->blk.cols);
-            TOMO_TRY(validate_items(items, n0, r.cd->pc.nx, st->blk.T, st->blk.cols));
+            const ProblemClass& pc = r.cd->pc;
+            append_items(items, r.first, r.nsolves, pc.nx, pc.ny, pc.nc, item_face_distance(pc), st->blk.T,
+                         st->blk.cols, nseg);
+            TOMO_TRY(validate_items(items, n0, pc.nx, pc.ny, st->blk.T, st->blk.cols));
         }
         st->nitems = (int)items.size();
         if (!items.empty()) {
