@@ -518,8 +518,9 @@ def main() -> None:
     ap.add_argument("--batch-min", type=int, default=2, help="serving: smallest candidate batch")
     ap.add_argument("--batch-max", type=int, default=16, help="serving: largest candidate batch")
     ap.add_argument("--utilisation", type=float, default=0.8, help="serving: offered load / capacity")
-    ap.add_argument("--rate-gcells", type=float, default=80.0,
-                    help="serving: assumed capacity (Gcell-updates/s) that sets the arrival rate")
+    ap.add_argument("--rate-gcells", type=float, default=120.0,
+                    help="serving: capacity (Gcell-updates/s, about the batch path's measured rate) that, "
+                         "with --utilisation, sets the arrival rate")
     args = ap.parse_args()
     if args.workload == "serving" and args.impl == "ours":
         run_serving(args)
