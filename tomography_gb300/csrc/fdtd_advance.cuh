@@ -410,359 +410,57 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
             }
         }
 
+        // ---- every level on an interior row (the common case): one straight-line
+        // block over all T levels, so the scheduler can interleave their
+        // independent dependency chains; the formulas are the fast path's
+        bool interior = !wspecial;
 #pragma unroll
-        for (int k = T - 1; k >= 0; --k) {
-            const int q = r - 2 * k;       // row received this iteration
-            const int m = q - 1;           // row advanced this iteration
-            Real iz[COLS], ix[COLS], iy[COLS], ij[COLS];
-            const uint32_t im = (k == 0) ? lm : hmat[k];
+        for (int k = 0; k < T; ++k) {
+            const int m = r - 2 * k - 1;
+            interior = interior && k < nsteps && m > nc && m < ny - nc && !((rowbits[m >> 5] >> (m & 31)) & 1u);
+        }
+        if (interior) {
 #pragma unroll
-            for (int c = 0; c < COLS; ++c) {
-                if (k == 0) { iz[c] = lz[c]; ix[c] = lx[c]; iy[c] = ly[c]; ij[c] = lj[c]; }
-                else { iz[c] = hz[k][c]; ix[c] = hxr[k][c]; iy[c] = hyr[k][c]; ij[c] = hj[k][c]; }
-            }
-            if (q < 0 || m > ny) continue;   // level idle (uniform)
-            if (m >= 0) {
+            for (int k = T - 1; k >= 0; --k) {
+                const int m = r - 2 * k - 1;
+                Real iz[COLS], ix[COLS], iy[COLS], ij[COLS];
+                const uint32_t im = (k == 0) ? lm : hmat[k];
+#pragma unroll
+                for (int c = 0; c < COLS; ++c) {
+                    if (k == 0) { iz[c] = lz[c]; ix[c] = lx[c]; iy[c] = ly[c]; ij[c] = lj[c]; }
+                    else { iz[c] = hz[k][c]; ix[c] = hxr[k][c]; iy[c] = hyr[k][c]; ij[c] = hj[k][c]; }
+                }
                 Real oz[COLS], ox[COLS], oy[COLS], oj[COLS];
-                const int n = n0 + k;        // time step index computed by this level
-                const bool rowbit = (rowbits[m >> 5] >> (m & 31)) & 1u;
-                const bool fast = !wspecial && !rowbit;
-                if (k < nsteps && fast) {
-                    // ================= fast path: interior Yee + Debye; in breast mode
-                    // also the rows of the y-CPML strips (row-uniform psi terms, the
-                    // general path's formulas; rows 0 and ny stay on the general path)
-                    const int iyh = kRef ? -1 : ((m < nc) ? nc - 1 - m : ((m >= ny - nc) ? m - ny + nc : -1));
-                    const int iye = kRef ? -1 : ((m <= nc) ? nc - m : ((m >= ny - nc) ? m - ny + nc : -1));
-                    const Real ezR_last = __shfl_down_sync(0xffffffffu, pz[k][0], 1);
+                const Real ezR_last = __shfl_down_sync(0xffffffffu, pz[k][0], 1);
 #pragma unroll
-                    for (int c = 0; c < COLS; ++c) {
-                        const Real ez0 = pz[k][c];
-                        const Real ezR = (c + 1 < COLS) ? pz[k][c + 1] : ezR_last;
-                        oy[c] = O::fma(chez, O::sub(ezR, ez0), py_[k][c]);
-                        const Real dEx = O::sub(iz[c], ez0);
-                        ox[c] = O::fma(-chez, dEx, px_[k][c]);
-                        if (iyh >= 0) {
-                            const int ysx = (m < nc) ? m : m - (ny - nc) + nc;
-                            const Real ps = O::fma(cpml[4 * nc + iyh], psi_in(k, 2, m, c), O::mul(cpml[5 * nc + iyh], dEx));
-                            psi_out(k, 2, m, c, ps, psy_h + (size_t)ysx * (nx + 1) + xcol[c]);
-                            ox[c] = O::fma(-O::mul(chez, dEx), cpml[3 * nc + iyh], px_[k][c]);
-                            ox[c] = O::fma(-O::mul(chez, dxr), ps, ox[c]);
-                        }
-                        if (clampnan) {
-                            if (dev_isnan(ox[c])) ox[c] = Real(0);
-                            if (dev_isnan(oy[c])) oy[c] = Real(0);
-                        }
-                    }
-                    const Real hyL_first = __shfl_up_sync(0xffffffffu, oy[COLS - 1], 1);
-#pragma unroll
-                    for (int c = 0; c < COLS; ++c) {
-                        const int mi = (pmat[k] >> (8 * c)) & kMatMask;
-                        Real Ca, Cb, Cj, Bp;
-                        load_coefs(ws.tab[mi], Ca, Cb, Cj, Bp);
-                        const Real hyL = (c > 0) ? oy[c - 1] : hyL_first;
-                        const Real dHy = O::sub(oy[c], hyL);
-                        const Real dHx = O::sub(ox[c], hxn[k][c]);
-                        const Real ez = pz[k][c], jp = pj[k][c];
-                        Real out;
-                        if (kRef) {
-                            out = O::fma(Ca, ez, O::sub(O::mul(Cb, dHy), O::mul(Cb, dHx)));
-                        } else if (iye >= 0) {
-                            const int ysx = (m <= nc) ? m - 1 : m - (ny - nc) + nc;
-                            const Real qy = O::fma(cpml[nc + iye], psi_in(k, 3, m, c), O::mul(cpml[2 * nc + iye], dHx));
-                            psi_out(k, 3, m, c, qy, psy_e + (size_t)ysx * (nx + 1) + xcol[c]);
-                            const Real cy = O::mul(dHx, cpml[iye]);
-                            out = O::fma(Ca, ez, O::mul(Cb, O::fma(dxr, O::sub(Real(0), qy), O::sub(dHy, cy))));
-                        } else {
-                            out = O::fma(Ca, ez, O::mul(Cb, O::sub(dHy, dHx)));
-                        }
-                        out = O::fma(-Cj, jp, out);
-                        oj[c] = O::fma(Kp, jp, O::mul(Bp, O::sub(out, ez)));
-                        if (clampnan && dev_isnan(out)) out = Real(0);
-                        oz[c] = out;
-                    }
-                } else if (kEdgePath && k < nsteps && !rowbit) {
-                    // ================= edge path (breast mode, narrow strips at the left
-                    // and right edges): the fast path's straight-line code with the
-                    // x-CPML terms computed branch-free on every lane and chosen per lane
-                    // by select, row-uniform y-CPML terms, and the PEC boundary and the
-                    // padding columns held by select.  Each value is chosen from the same
-                    // explicitly rounded formulas the general path evaluates, so every
-                    // cell gets the same bits.  (Values computed for lanes that do not
-                    // select them may come from stale shared memory; they are discarded.)
-                    const int iyh = (m < nc) ? nc - 1 - m : ((m >= ny - nc) ? m - ny + nc : -1);
-                    const int iye = (m <= nc) ? nc - m : ((m >= ny - nc) ? m - ny + nc : -1);
-                    const Real ezR_last = __shfl_down_sync(0xffffffffu, pz[k][0], 1);
-#pragma unroll
-                    for (int c = 0; c < COLS; ++c) {
-                        const int x = xcol[c];
-                        const bool hin = x >= 0 && x < nx;
-                        const bool isx = ixh[c] >= 0;
-                        const int i = isx ? ixh[c] : 0;
-                        const Real ez0 = pz[k][c];
-                        const Real ezR = (c + 1 < COLS) ? pz[k][c + 1] : ezR_last;
-                        const Real hx0 = px_[k][c], hy0 = py_[k][c];
-                        const Real dEy = O::sub(ezR, ez0);
-                        const Real dEx = O::sub(iz[c], ez0);
-                        Real hy = O::fma(chez, dEy, hy0);
-                        Real hx = O::fma(-chez, dEx, hx0);
-                        const Real psx = O::fma(cpml[4 * nc + i], psi_in(k, 0, m, c), O::mul(cpml[5 * nc + i], dEy));
-                        Real hyc = O::fma(O::mul(chez, dEy), cpml[3 * nc + i], hy0);
-                        hyc = O::fma(O::mul(chez, dxr), psx, hyc);
-                        if (isx) {
-                            const int xsx = (x < nc) ? x : x - (nx - nc) + nc;
-                            psi_out(k, 0, m, c, psx, psx_h + (size_t)m * 2 * nc + xsx);
-                        }
-                        hy = isx ? hyc : hy;
-                        if (iyh >= 0) {
-                            const int ysx = (m < nc) ? m : m - (ny - nc) + nc;
-                            const Real ps = O::fma(cpml[4 * nc + iyh], psi_in(k, 2, m, c), O::mul(cpml[5 * nc + iyh], dEx));
-                            if (hin) psi_out(k, 2, m, c, ps, psy_h + (size_t)ysx * (nx + 1) + x);
-                            hx = O::fma(-O::mul(chez, dEx), cpml[3 * nc + iyh], hx0);
-                            hx = O::fma(-O::mul(chez, dxr), ps, hx);
-                        }
-                        ox[c] = hin ? hx : hx0;
-                        oy[c] = hin ? hy : hy0;
-                    }
-                    const Real hyL_first = __shfl_up_sync(0xffffffffu, oy[COLS - 1], 1);
-#pragma unroll
-                    for (int c = 0; c < COLS; ++c) {
-                        const int x = xcol[c];
-                        const bool ein = x >= 1 && x <= nx - 1;
-                        const bool isx = ixe[c] >= 0;
-                        const int i = isx ? ixe[c] : 0;
-                        const int mi = (pmat[k] >> (8 * c)) & kMatMask;
-                        Real Ca, Cb, Cj, Bp;
-                        load_coefs(ws.tab[mi], Ca, Cb, Cj, Bp);
-                        const Real hyL = (c > 0) ? oy[c - 1] : hyL_first;
-                        const Real dHy = O::sub(oy[c], hyL);
-                        const Real dHx = O::sub(ox[c], hxn[k][c]);
-                        const Real ez = pz[k][c], jp = pj[k][c];
-                        const Real qxc = O::fma(cpml[nc + i], psi_in(k, 1, m, c), O::mul(cpml[2 * nc + i], dHy));
-                        if (isx) {
-                            const int xsx = (x <= nc) ? x - 1 : x - (nx - nc) + nc;
-                            psi_out(k, 1, m, c, qxc, psx_e + (size_t)m * 2 * nc + xsx);
-                        }
-                        const Real cxc = O::mul(dHy, cpml[i]);
-                        const Real qx = isx ? qxc : Real(0);
-                        const Real cx = isx ? cxc : dHy;
-                        Real qy = Real(0), cy = dHx;
-                        if (iye >= 0) {
-                            const int ysx = (m <= nc) ? m - 1 : m - (ny - nc) + nc;
-                            qy = O::fma(cpml[nc + iye], psi_in(k, 3, m, c), O::mul(cpml[2 * nc + iye], dHx));
-                            if (ein) psi_out(k, 3, m, c, qy, psy_e + (size_t)ysx * (nx + 1) + x);
-                            cy = O::mul(dHx, cpml[iye]);
-                        }
-                        const Real outc = O::fma(Ca, ez, O::mul(Cb, O::fma(dxr, O::sub(qx, qy), O::sub(cx, cy))));
-                        const Real outp = O::fma(Ca, ez, O::mul(Cb, O::sub(dHy, dHx)));
-                        Real out = (isx || iye >= 0) ? outc : outp;
-                        out = O::fma(-Cj, jp, out);
-                        const Real jpo = O::fma(Kp, jp, O::mul(Bp, O::sub(out, ez)));
-                        oz[c] = ein ? out : Real(0);
-                        oj[c] = ein ? jpo : jp;
-                    }
-                    // vertical NTFF faces: buffer (h, e) samples for the warp-wide flush
-                    if (nfreq > 0 && (has_face0 || has_face1) && m >= fd && m <= ny - fd - 1) {
-                        const Real ezR2_last = __shfl_down_sync(0xffffffffu, oz[0], 1);
-#pragma unroll
-                        for (int c = 0; c < COLS; ++c) {
-                            if (face_slot[c] >= 0) {
-                                const Real ezR2 = (c + 1 < COLS) ? oz[c + 1] : ezR2_last;
-                                Real* smp = ws.ring[face_slot[c]][m % kRing][k];
-                                smp[0] = oy[c];
-                                smp[1] = O::mul(O::add(oz[c], ezR2), Real(0.5));
-                            }
-                        }
-                    }
-                } else if (k < nsteps) {
-                    // ================= general path
-                    const bool hrow = m < ny;
-                    const int iyh = (m < nc) ? nc - 1 - m : ((m >= ny - nc && m < ny) ? m - ny + nc : -1);
-                    Real ezR_last = __shfl_down_sync(0xffffffffu, pz[k][0], 1);
-#pragma unroll
-                    for (int c = 0; c < COLS; ++c) {
-                        const int x = xcol[c];
-                        Real ez0 = pz[k][c];
-                        Real ezR = (c + 1 < COLS) ? pz[k][c + 1] : ezR_last;
-                        Real hx0 = px_[k][c], hy0 = py_[k][c];
-                        Real hx = hx0, hy = hy0;
-                        if (hrow && x >= 0 && x < nx) {
-                            Real dEy = O::sub(ezR, ez0);
-                            Real dEx = O::sub(iz[c], ez0);
-                            hy = O::fma(chez, dEy, hy0);
-                            hx = O::fma(-chez, dEx, hx0);
-                            if (ixh[c] >= 0) {
-                                const int i = ixh[c];
-                                const int xsx = (x < nc) ? x : x - (nx - nc) + nc;
-                                Real ps = O::fma(cpml[4 * nc + i], psi_in(k, 0, m, c), O::mul(cpml[5 * nc + i], dEy));
-                                psi_out(k, 0, m, c, ps, psx_h + (size_t)m * 2 * nc + xsx);
-                                hy = O::fma(O::mul(chez, dEy), cpml[3 * nc + i], hy0);
-                                hy = O::fma(O::mul(chez, dxr), ps, hy);
-                            }
-                            if (iyh >= 0) {
-                                const int ysx = (m < nc) ? m : m - (ny - nc) + nc;
-                                Real ps = O::fma(cpml[4 * nc + iyh], psi_in(k, 2, m, c), O::mul(cpml[5 * nc + iyh], dEx));
-                                psi_out(k, 2, m, c, ps, psy_h + (size_t)ysx * (nx + 1) + x);
-                                hx = O::fma(-O::mul(chez, dEx), cpml[3 * nc + iyh], hx0);
-                                hx = O::fma(-O::mul(chez, dxr), ps, hx);
-                            }
-                            if (clampnan) {
-                                if (dev_isnan(hx)) hx = Real(0);
-                                if (dev_isnan(hy)) hy = Real(0);
-                            }
-                        }
-                        ox[c] = hx;
-                        oy[c] = hy;
-                    }
-                    Real hyL_first = __shfl_up_sync(0xffffffffu, oy[COLS - 1], 1);
-                    const bool erow = m >= 1 && m <= ny - 1;
-                    const int iye = (m >= 1 && m <= nc) ? nc - m : ((m >= ny - nc && m <= ny - 1) ? m - ny + nc : -1);
-#pragma unroll
-                    for (int c = 0; c < COLS; ++c) {
-                        const int x = xcol[c];
-                        Real ez = pz[k][c];
-                        Real jp = pj[k][c];
-                        Real out = Real(0);
-                        Real jpo = jp;
-                        if (erow && x >= 1 && x <= nx - 1) {
-                            const uint32_t mb = (pmat[k] >> (8 * c)) & 0xffu;
-                            const int mi = mb & kMatMask;
-                            const Real* cf = D.mtab + mi * kMatCoef;     // cold columns (global, cached)
-                            Real Ca, Cb, Cj, Bp;
-                            load_coefs(ws.tab[mi], Ca, Cb, Cj, Bp);
-                            Real hyL = (c > 0) ? oy[c - 1] : hyL_first;
-                            Real dHy = O::sub(oy[c], hyL);
-                            Real dHx = O::sub(ox[c], hxn[k][c]);
-                            Real gp = Real(0), gm = Real(0);
-                            if (kRef) {
-                                const Real Ci = cf[kCi], Cp = cf[kCp];
-                                if (Ci != Real(0) || Cp != Real(0) || Bp != Real(0)) {
-                                    // fwf() argument in FP64 (FDTD_GPU.cu:290): time minus the
-                                    // projected travel time of the incident front to this cell
-                                    const double b = __dmul_rn(__dadd_rn(__dmul_rn(D.pw_ky, (double)m - D.pw_yoff),
-                                                                         __dmul_rn(D.pw_kx, (double)x - D.pw_xoff)),
-                                                               D.pw_dxc0);
-                                    const double a0 = __dsub_rn(__dsub_rn(__dmul_rn((double)n + 0.5, D.dt), D.pw_t0l), b);
-                                    const double a1 = __dsub_rn(__dsub_rn(__dmul_rn((double)n - 0.5, D.dt), D.pw_t0l), b);
-                                    Real u0 = (Real)__dmul_rn(a0, D.pw_inv_tau), u1 = (Real)__dmul_rn(a1, D.pw_inv_tau);
-                                    gp = dev_exp<Real>(-O::mul(u0, u0));
-                                    gm = dev_exp<Real>(-O::mul(u1, u1));
-                                }
-                                // FDTD_GPU.cu:378-385 (interior), then the strip overrides :389-416
-                                out = O::fma(Ca, ez, O::sub(O::mul(Cb, dHy), O::mul(Cb, dHx)));
-                                out = O::fma(cf[kCi], gp, O::fma(cf[kCp], gm, out));
-                                out = O::fma(-Cj, jp, out);
-                                jpo = O::fma(Kp, jp, O::mul(Bp, O::add(O::sub(out, ez), O::sub(gp, gm))));
-                                if (ixe[c] >= 0) {
-                                    const int i = ixe[c];
-                                    const int xsx = (x <= nc) ? x - 1 : x - (nx - nc) + nc;
-                                    Real ps = O::fma(cpml[nc + i], psi_in(k, 1, m, c), O::mul(cpml[2 * nc + i], dHy));
-                                    psi_out(k, 1, m, c, ps, psx_e + (size_t)m * 2 * nc + xsx);
-                                    const Real rk = cpml[i];
-                                    out = O::fma(Ca, ez, O::mul(O::mul(Cb, O::sub(dHy, dHx)), rk));
-                                    out = O::fma(O::mul(Cb, dxr), ps, out);
-                                }
-                                if (iye >= 0) {
-                                    const int ysx = (m <= nc) ? m - 1 : m - (ny - nc) + nc;
-                                    Real ps = O::fma(cpml[nc + iye], psi_in(k, 3, m, c), O::mul(cpml[2 * nc + iye], dHx));
-                                    psi_out(k, 3, m, c, ps, psy_e + (size_t)ysx * (nx + 1) + x);
-                                    const Real rk = cpml[iye];
-                                    out = O::fma(Ca, ez, O::mul(O::mul(Cb, O::sub(dHy, dHx)), rk));
-                                    out = O::fma(-O::mul(Cb, dxr), ps, out);
-                                }
-                            } else {
-                                Real cx = dHy, cy = dHx, qx = Real(0), qy = Real(0);
-                                if (ixe[c] >= 0) {
-                                    const int i = ixe[c];
-                                    const int xsx = (x <= nc) ? x - 1 : x - (nx - nc) + nc;
-                                    qx = O::fma(cpml[nc + i], psi_in(k, 1, m, c), O::mul(cpml[2 * nc + i], dHy));
-                                    psi_out(k, 1, m, c, qx, psx_e + (size_t)m * 2 * nc + xsx);
-                                    cx = O::mul(dHy, cpml[i]);
-                                }
-                                if (iye >= 0) {
-                                    const int ysx = (m <= nc) ? m - 1 : m - (ny - nc) + nc;
-                                    qy = O::fma(cpml[nc + iye], psi_in(k, 3, m, c), O::mul(cpml[2 * nc + iye], dHx));
-                                    psi_out(k, 3, m, c, qy, psy_e + (size_t)ysx * (nx + 1) + x);
-                                    cy = O::mul(dHx, cpml[iye]);
-                                }
-                                // proper CPML: both stretched derivatives and both psi terms
-                                if (ixe[c] >= 0 || iye >= 0)
-                                    out = O::fma(Ca, ez, O::mul(Cb, O::fma(dxr, O::sub(qx, qy), O::sub(cx, cy))));
-                                else
-                                    out = O::fma(Ca, ez, O::mul(Cb, O::sub(dHy, dHx)));
-                                out = O::fma(-Cj, jp, out);
-                                if (psrc && m == src_y && x == src_x) out = O::fma(cf[kCs], D.src_wave[n], out);
-                                jpo = O::fma(Kp, jp, O::mul(Bp, O::sub(out, ez)));
-                            }
-                            if (clampnan && dev_isnan(out)) out = Real(0);
-                            // receivers (owned cells only, so each sample is written once)
-                            if ((mb & kMatRx) && owned[c] && m >= y0 && m < y1) {
-                                for (int rr = 0; rr < D.nrx; ++rr)
-                                    if (D.rx[2 * rr] == x && D.rx[2 * rr + 1] == m)
-                                        D.traces[(size_t)rr * S + n] = out;
-                            }
-                        }
-                        oz[c] = out;
-                        oj[c] = jpo;
-                    }
-                    // running DFT on the NTFF contour
-                    if (nfreq > 0) {
-                        const Real* ph = phasor + (size_t)n * nfreq * 4;
-                        // horizontal faces: face row m-1 is complete at this level
-                        if ((m - 1 == fd || m - 1 == ny - fd - 1) && m - 1 >= y0 && m - 1 < y1) {
-                            const bool yp = (m - 1 == ny - fd - 1);
-#pragma unroll
-                            for (int c = 0; c < COLS; ++c) {
-                                const int x = xcol[c];
-                                if (owned[c] && x >= fd + 1 && x <= nx - fd - 2) {
-                                    Real e = O::mul(O::add(ezn[k][c], oz[c]), Real(0.5));
-                                    Real h = hxn[k][c];
-                                    int ci = yp ? contour_index_yp(nx, ny, fd, x) : contour_index_yn(nx, ny, fd, x);
-                                    if (yp) { e = -e; h = -h; }
-                                    dft_update(acc, ph, nfreq, C, ci, h, e);
-                                }
-                            }
-                        }
-                        // vertical faces: buffer (h, e) samples per row for a warp-wide flush
-                        if ((has_face0 || has_face1) && m >= fd && m <= ny - fd - 1) {
-                            Real ezR2_last = __shfl_down_sync(0xffffffffu, oz[0], 1);
-#pragma unroll
-                            for (int c = 0; c < COLS; ++c) {
-                                if (face_slot[c] >= 0) {
-                                    Real ezR2 = (c + 1 < COLS) ? oz[c + 1] : ezR2_last;
-                                    Real e = O::mul(O::add(oz[c], ezR2), Real(0.5));
-                                    Real* s = ws.ring[face_slot[c]][m % kRing][k];
-                                    s[0] = oy[c];
-                                    s[1] = e;
-                                }
-                            }
-                        }
-                    }
-                } else {
-                    // beyond the last time step: pass through unchanged (psi included)
-#pragma unroll
-                    for (int c = 0; c < COLS; ++c) {
-                        oz[c] = pz[k][c]; ox[c] = px_[k][c]; oy[c] = py_[k][c]; oj[c] = pj[k][c];
-                        const int x = xcol[c];
-                        if (ixh[c] >= 0 && m < ny) {
-                            const int xsx = (x < nc) ? x : x - (nx - nc) + nc;
-                            psi_out(k, 0, m, c, psi_in(k, 0, m, c), psx_h + (size_t)m * 2 * nc + xsx);
-                        }
-                        if (ixe[c] >= 0 && m >= 1 && m <= ny - 1) {
-                            const int xsx = (x <= nc) ? x - 1 : x - (nx - nc) + nc;
-                            psi_out(k, 1, m, c, psi_in(k, 1, m, c), psx_e + (size_t)m * 2 * nc + xsx);
-                        }
-                        if (x >= 0 && x <= nx) {
-                            const int iyh = (m < nc) ? m : ((m >= ny - nc && m < ny) ? m - (ny - nc) + nc : -1);
-                            if (iyh >= 0 && x < nx)
-                                psi_out(k, 2, m, c, psi_in(k, 2, m, c), psy_h + (size_t)iyh * (nx + 1) + x);
-                            const int iye = (m >= 1 && m <= nc) ? m - 1
-                                            : ((m >= ny - nc && m <= ny - 1) ? m - (ny - nc) + nc : -1);
-                            if (iye >= 0 && x >= 1 && x <= nx - 1)
-                                psi_out(k, 3, m, c, psi_in(k, 3, m, c), psy_e + (size_t)iye * (nx + 1) + x);
-                        }
+                for (int c = 0; c < COLS; ++c) {
+                    const Real ez0 = pz[k][c];
+                    const Real ezR = (c + 1 < COLS) ? pz[k][c + 1] : ezR_last;
+                    oy[c] = O::fma(chez, O::sub(ezR, ez0), py_[k][c]);
+                    ox[c] = O::fma(-chez, O::sub(iz[c], ez0), px_[k][c]);
+                    if (clampnan) {
+                        if (dev_isnan(ox[c])) ox[c] = Real(0);
+                        if (dev_isnan(oy[c])) oy[c] = Real(0);
                     }
                 }
-                // ---- emit row m
+                const Real hyL_first = __shfl_up_sync(0xffffffffu, oy[COLS - 1], 1);
+#pragma unroll
+                for (int c = 0; c < COLS; ++c) {
+                    const int mi = (pmat[k] >> (8 * c)) & kMatMask;
+                    Real Ca, Cb, Cj, Bp;
+                    load_coefs(ws.tab[mi], Ca, Cb, Cj, Bp);
+                    const Real hyL = (c > 0) ? oy[c - 1] : hyL_first;
+                    const Real dHy = O::sub(oy[c], hyL);
+                    const Real dHx = O::sub(ox[c], hxn[k][c]);
+                    const Real ez = pz[k][c], jp = pj[k][c];
+                    Real out;
+                    if (kRef) out = O::fma(Ca, ez, O::sub(O::mul(Cb, dHy), O::mul(Cb, dHx)));
+                    else out = O::fma(Ca, ez, O::mul(Cb, O::sub(dHy, dHx)));
+                    out = O::fma(-Cj, jp, out);
+                    oj[c] = O::fma(Kp, jp, O::mul(Bp, O::sub(out, ez)));
+                    if (clampnan && dev_isnan(out)) out = Real(0);
+                    oz[c] = out;
+                }
 #pragma unroll
                 for (int c = 0; c < COLS; ++c) {
                     hxn[k][c] = ox[c];
@@ -788,12 +486,398 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
                         }
                     }
                 }
-            }
-            // the received row becomes this level's previous row
-            pmat[k] = im;
+                pmat[k] = im;
 #pragma unroll
-            for (int c = 0; c < COLS; ++c) {
-                pz[k][c] = iz[c]; px_[k][c] = ix[c]; py_[k][c] = iy[c]; pj[k][c] = ij[c];
+                for (int c = 0; c < COLS; ++c) {
+                    pz[k][c] = iz[c]; px_[k][c] = ix[c]; py_[k][c] = iy[c]; pj[k][c] = ij[c];
+                }
+            }
+        } else {
+#pragma unroll
+            for (int k = T - 1; k >= 0; --k) {
+                const int q = r - 2 * k;       // row received this iteration
+                const int m = q - 1;           // row advanced this iteration
+                Real iz[COLS], ix[COLS], iy[COLS], ij[COLS];
+                const uint32_t im = (k == 0) ? lm : hmat[k];
+#pragma unroll
+                for (int c = 0; c < COLS; ++c) {
+                    if (k == 0) { iz[c] = lz[c]; ix[c] = lx[c]; iy[c] = ly[c]; ij[c] = lj[c]; }
+                    else { iz[c] = hz[k][c]; ix[c] = hxr[k][c]; iy[c] = hyr[k][c]; ij[c] = hj[k][c]; }
+                }
+                if (q < 0 || m > ny) continue;   // level idle (uniform)
+                if (m >= 0) {
+                    Real oz[COLS], ox[COLS], oy[COLS], oj[COLS];
+                    const int n = n0 + k;        // time step index computed by this level
+                    const bool rowbit = (rowbits[m >> 5] >> (m & 31)) & 1u;
+                    const bool fast = !wspecial && !rowbit;
+                    if (k < nsteps && fast) {
+                        // ================= fast path: interior Yee + Debye; in breast mode
+                        // also the rows of the y-CPML strips (row-uniform psi terms, the
+                        // general path's formulas; rows 0 and ny stay on the general path)
+                        const int iyh = kRef ? -1 : ((m < nc) ? nc - 1 - m : ((m >= ny - nc) ? m - ny + nc : -1));
+                        const int iye = kRef ? -1 : ((m <= nc) ? nc - m : ((m >= ny - nc) ? m - ny + nc : -1));
+                        const Real ezR_last = __shfl_down_sync(0xffffffffu, pz[k][0], 1);
+#pragma unroll
+                        for (int c = 0; c < COLS; ++c) {
+                            const Real ez0 = pz[k][c];
+                            const Real ezR = (c + 1 < COLS) ? pz[k][c + 1] : ezR_last;
+                            oy[c] = O::fma(chez, O::sub(ezR, ez0), py_[k][c]);
+                            const Real dEx = O::sub(iz[c], ez0);
+                            ox[c] = O::fma(-chez, dEx, px_[k][c]);
+                            if (iyh >= 0) {
+                                const int ysx = (m < nc) ? m : m - (ny - nc) + nc;
+                                const Real ps = O::fma(cpml[4 * nc + iyh], psi_in(k, 2, m, c), O::mul(cpml[5 * nc + iyh], dEx));
+                                psi_out(k, 2, m, c, ps, psy_h + (size_t)ysx * (nx + 1) + xcol[c]);
+                                ox[c] = O::fma(-O::mul(chez, dEx), cpml[3 * nc + iyh], px_[k][c]);
+                                ox[c] = O::fma(-O::mul(chez, dxr), ps, ox[c]);
+                            }
+                            if (clampnan) {
+                                if (dev_isnan(ox[c])) ox[c] = Real(0);
+                                if (dev_isnan(oy[c])) oy[c] = Real(0);
+                            }
+                        }
+                        const Real hyL_first = __shfl_up_sync(0xffffffffu, oy[COLS - 1], 1);
+#pragma unroll
+                        for (int c = 0; c < COLS; ++c) {
+                            const int mi = (pmat[k] >> (8 * c)) & kMatMask;
+                            Real Ca, Cb, Cj, Bp;
+                            load_coefs(ws.tab[mi], Ca, Cb, Cj, Bp);
+                            const Real hyL = (c > 0) ? oy[c - 1] : hyL_first;
+                            const Real dHy = O::sub(oy[c], hyL);
+                            const Real dHx = O::sub(ox[c], hxn[k][c]);
+                            const Real ez = pz[k][c], jp = pj[k][c];
+                            Real out;
+                            if (kRef) {
+                                out = O::fma(Ca, ez, O::sub(O::mul(Cb, dHy), O::mul(Cb, dHx)));
+                            } else if (iye >= 0) {
+                                const int ysx = (m <= nc) ? m - 1 : m - (ny - nc) + nc;
+                                const Real qy = O::fma(cpml[nc + iye], psi_in(k, 3, m, c), O::mul(cpml[2 * nc + iye], dHx));
+                                psi_out(k, 3, m, c, qy, psy_e + (size_t)ysx * (nx + 1) + xcol[c]);
+                                const Real cy = O::mul(dHx, cpml[iye]);
+                                out = O::fma(Ca, ez, O::mul(Cb, O::fma(dxr, O::sub(Real(0), qy), O::sub(dHy, cy))));
+                            } else {
+                                out = O::fma(Ca, ez, O::mul(Cb, O::sub(dHy, dHx)));
+                            }
+                            out = O::fma(-Cj, jp, out);
+                            oj[c] = O::fma(Kp, jp, O::mul(Bp, O::sub(out, ez)));
+                            if (clampnan && dev_isnan(out)) out = Real(0);
+                            oz[c] = out;
+                        }
+                    } else if (kEdgePath && k < nsteps && !rowbit) {
+                        // ================= edge path (breast mode, narrow strips at the left
+                        // and right edges): the fast path's straight-line code with the
+                        // x-CPML terms computed branch-free on every lane and chosen per lane
+                        // by select, row-uniform y-CPML terms, and the PEC boundary and the
+                        // padding columns held by select.  Each value is chosen from the same
+                        // explicitly rounded formulas the general path evaluates, so every
+                        // cell gets the same bits.  (Values computed for lanes that do not
+                        // select them may come from stale shared memory; they are discarded.)
+                        const int iyh = (m < nc) ? nc - 1 - m : ((m >= ny - nc) ? m - ny + nc : -1);
+                        const int iye = (m <= nc) ? nc - m : ((m >= ny - nc) ? m - ny + nc : -1);
+                        const Real ezR_last = __shfl_down_sync(0xffffffffu, pz[k][0], 1);
+#pragma unroll
+                        for (int c = 0; c < COLS; ++c) {
+                            const int x = xcol[c];
+                            const bool hin = x >= 0 && x < nx;
+                            const bool isx = ixh[c] >= 0;
+                            const int i = isx ? ixh[c] : 0;
+                            const Real ez0 = pz[k][c];
+                            const Real ezR = (c + 1 < COLS) ? pz[k][c + 1] : ezR_last;
+                            const Real hx0 = px_[k][c], hy0 = py_[k][c];
+                            const Real dEy = O::sub(ezR, ez0);
+                            const Real dEx = O::sub(iz[c], ez0);
+                            Real hy = O::fma(chez, dEy, hy0);
+                            Real hx = O::fma(-chez, dEx, hx0);
+                            const Real psx = O::fma(cpml[4 * nc + i], psi_in(k, 0, m, c), O::mul(cpml[5 * nc + i], dEy));
+                            Real hyc = O::fma(O::mul(chez, dEy), cpml[3 * nc + i], hy0);
+                            hyc = O::fma(O::mul(chez, dxr), psx, hyc);
+                            if (isx) {
+                                const int xsx = (x < nc) ? x : x - (nx - nc) + nc;
+                                psi_out(k, 0, m, c, psx, psx_h + (size_t)m * 2 * nc + xsx);
+                            }
+                            hy = isx ? hyc : hy;
+                            if (iyh >= 0) {
+                                const int ysx = (m < nc) ? m : m - (ny - nc) + nc;
+                                const Real ps = O::fma(cpml[4 * nc + iyh], psi_in(k, 2, m, c), O::mul(cpml[5 * nc + iyh], dEx));
+                                if (hin) psi_out(k, 2, m, c, ps, psy_h + (size_t)ysx * (nx + 1) + x);
+                                hx = O::fma(-O::mul(chez, dEx), cpml[3 * nc + iyh], hx0);
+                                hx = O::fma(-O::mul(chez, dxr), ps, hx);
+                            }
+                            ox[c] = hin ? hx : hx0;
+                            oy[c] = hin ? hy : hy0;
+                        }
+                        const Real hyL_first = __shfl_up_sync(0xffffffffu, oy[COLS - 1], 1);
+#pragma unroll
+                        for (int c = 0; c < COLS; ++c) {
+                            const int x = xcol[c];
+                            const bool ein = x >= 1 && x <= nx - 1;
+                            const bool isx = ixe[c] >= 0;
+                            const int i = isx ? ixe[c] : 0;
+                            const int mi = (pmat[k] >> (8 * c)) & kMatMask;
+                            Real Ca, Cb, Cj, Bp;
+                            load_coefs(ws.tab[mi], Ca, Cb, Cj, Bp);
+                            const Real hyL = (c > 0) ? oy[c - 1] : hyL_first;
+                            const Real dHy = O::sub(oy[c], hyL);
+                            const Real dHx = O::sub(ox[c], hxn[k][c]);
+                            const Real ez = pz[k][c], jp = pj[k][c];
+                            const Real qxc = O::fma(cpml[nc + i], psi_in(k, 1, m, c), O::mul(cpml[2 * nc + i], dHy));
+                            if (isx) {
+                                const int xsx = (x <= nc) ? x - 1 : x - (nx - nc) + nc;
+                                psi_out(k, 1, m, c, qxc, psx_e + (size_t)m * 2 * nc + xsx);
+                            }
+                            const Real cxc = O::mul(dHy, cpml[i]);
+                            const Real qx = isx ? qxc : Real(0);
+                            const Real cx = isx ? cxc : dHy;
+                            Real qy = Real(0), cy = dHx;
+                            if (iye >= 0) {
+                                const int ysx = (m <= nc) ? m - 1 : m - (ny - nc) + nc;
+                                qy = O::fma(cpml[nc + iye], psi_in(k, 3, m, c), O::mul(cpml[2 * nc + iye], dHx));
+                                if (ein) psi_out(k, 3, m, c, qy, psy_e + (size_t)ysx * (nx + 1) + x);
+                                cy = O::mul(dHx, cpml[iye]);
+                            }
+                            const Real outc = O::fma(Ca, ez, O::mul(Cb, O::fma(dxr, O::sub(qx, qy), O::sub(cx, cy))));
+                            const Real outp = O::fma(Ca, ez, O::mul(Cb, O::sub(dHy, dHx)));
+                            Real out = (isx || iye >= 0) ? outc : outp;
+                            out = O::fma(-Cj, jp, out);
+                            const Real jpo = O::fma(Kp, jp, O::mul(Bp, O::sub(out, ez)));
+                            oz[c] = ein ? out : Real(0);
+                            oj[c] = ein ? jpo : jp;
+                        }
+                        // vertical NTFF faces: buffer (h, e) samples for the warp-wide flush
+                        if (nfreq > 0 && (has_face0 || has_face1) && m >= fd && m <= ny - fd - 1) {
+                            const Real ezR2_last = __shfl_down_sync(0xffffffffu, oz[0], 1);
+#pragma unroll
+                            for (int c = 0; c < COLS; ++c) {
+                                if (face_slot[c] >= 0) {
+                                    const Real ezR2 = (c + 1 < COLS) ? oz[c + 1] : ezR2_last;
+                                    Real* smp = ws.ring[face_slot[c]][m % kRing][k];
+                                    smp[0] = oy[c];
+                                    smp[1] = O::mul(O::add(oz[c], ezR2), Real(0.5));
+                                }
+                            }
+                        }
+                    } else if (k < nsteps) {
+                        // ================= general path
+                        const bool hrow = m < ny;
+                        const int iyh = (m < nc) ? nc - 1 - m : ((m >= ny - nc && m < ny) ? m - ny + nc : -1);
+                        Real ezR_last = __shfl_down_sync(0xffffffffu, pz[k][0], 1);
+#pragma unroll
+                        for (int c = 0; c < COLS; ++c) {
+                            const int x = xcol[c];
+                            Real ez0 = pz[k][c];
+                            Real ezR = (c + 1 < COLS) ? pz[k][c + 1] : ezR_last;
+                            Real hx0 = px_[k][c], hy0 = py_[k][c];
+                            Real hx = hx0, hy = hy0;
+                            if (hrow && x >= 0 && x < nx) {
+                                Real dEy = O::sub(ezR, ez0);
+                                Real dEx = O::sub(iz[c], ez0);
+                                hy = O::fma(chez, dEy, hy0);
+                                hx = O::fma(-chez, dEx, hx0);
+                                if (ixh[c] >= 0) {
+                                    const int i = ixh[c];
+                                    const int xsx = (x < nc) ? x : x - (nx - nc) + nc;
+                                    Real ps = O::fma(cpml[4 * nc + i], psi_in(k, 0, m, c), O::mul(cpml[5 * nc + i], dEy));
+                                    psi_out(k, 0, m, c, ps, psx_h + (size_t)m * 2 * nc + xsx);
+                                    hy = O::fma(O::mul(chez, dEy), cpml[3 * nc + i], hy0);
+                                    hy = O::fma(O::mul(chez, dxr), ps, hy);
+                                }
+                                if (iyh >= 0) {
+                                    const int ysx = (m < nc) ? m : m - (ny - nc) + nc;
+                                    Real ps = O::fma(cpml[4 * nc + iyh], psi_in(k, 2, m, c), O::mul(cpml[5 * nc + iyh], dEx));
+                                    psi_out(k, 2, m, c, ps, psy_h + (size_t)ysx * (nx + 1) + x);
+                                    hx = O::fma(-O::mul(chez, dEx), cpml[3 * nc + iyh], hx0);
+                                    hx = O::fma(-O::mul(chez, dxr), ps, hx);
+                                }
+                                if (clampnan) {
+                                    if (dev_isnan(hx)) hx = Real(0);
+                                    if (dev_isnan(hy)) hy = Real(0);
+                                }
+                            }
+                            ox[c] = hx;
+                            oy[c] = hy;
+                        }
+                        Real hyL_first = __shfl_up_sync(0xffffffffu, oy[COLS - 1], 1);
+                        const bool erow = m >= 1 && m <= ny - 1;
+                        const int iye = (m >= 1 && m <= nc) ? nc - m : ((m >= ny - nc && m <= ny - 1) ? m - ny + nc : -1);
+#pragma unroll
+                        for (int c = 0; c < COLS; ++c) {
+                            const int x = xcol[c];
+                            Real ez = pz[k][c];
+                            Real jp = pj[k][c];
+                            Real out = Real(0);
+                            Real jpo = jp;
+                            if (erow && x >= 1 && x <= nx - 1) {
+                                const uint32_t mb = (pmat[k] >> (8 * c)) & 0xffu;
+                                const int mi = mb & kMatMask;
+                                const Real* cf = D.mtab + mi * kMatCoef;     // cold columns (global, cached)
+                                Real Ca, Cb, Cj, Bp;
+                                load_coefs(ws.tab[mi], Ca, Cb, Cj, Bp);
+                                Real hyL = (c > 0) ? oy[c - 1] : hyL_first;
+                                Real dHy = O::sub(oy[c], hyL);
+                                Real dHx = O::sub(ox[c], hxn[k][c]);
+                                Real gp = Real(0), gm = Real(0);
+                                if (kRef) {
+                                    const Real Ci = cf[kCi], Cp = cf[kCp];
+                                    if (Ci != Real(0) || Cp != Real(0) || Bp != Real(0)) {
+                                        // fwf() argument in FP64 (FDTD_GPU.cu:290): time minus the
+                                        // projected travel time of the incident front to this cell
+                                        const double b = __dmul_rn(__dadd_rn(__dmul_rn(D.pw_ky, (double)m - D.pw_yoff),
+                                                                             __dmul_rn(D.pw_kx, (double)x - D.pw_xoff)),
+                                                                   D.pw_dxc0);
+                                        const double a0 = __dsub_rn(__dsub_rn(__dmul_rn((double)n + 0.5, D.dt), D.pw_t0l), b);
+                                        const double a1 = __dsub_rn(__dsub_rn(__dmul_rn((double)n - 0.5, D.dt), D.pw_t0l), b);
+                                        Real u0 = (Real)__dmul_rn(a0, D.pw_inv_tau), u1 = (Real)__dmul_rn(a1, D.pw_inv_tau);
+                                        gp = dev_exp<Real>(-O::mul(u0, u0));
+                                        gm = dev_exp<Real>(-O::mul(u1, u1));
+                                    }
+                                    // FDTD_GPU.cu:378-385 (interior), then the strip overrides :389-416
+                                    out = O::fma(Ca, ez, O::sub(O::mul(Cb, dHy), O::mul(Cb, dHx)));
+                                    out = O::fma(cf[kCi], gp, O::fma(cf[kCp], gm, out));
+                                    out = O::fma(-Cj, jp, out);
+                                    jpo = O::fma(Kp, jp, O::mul(Bp, O::add(O::sub(out, ez), O::sub(gp, gm))));
+                                    if (ixe[c] >= 0) {
+                                        const int i = ixe[c];
+                                        const int xsx = (x <= nc) ? x - 1 : x - (nx - nc) + nc;
+                                        Real ps = O::fma(cpml[nc + i], psi_in(k, 1, m, c), O::mul(cpml[2 * nc + i], dHy));
+                                        psi_out(k, 1, m, c, ps, psx_e + (size_t)m * 2 * nc + xsx);
+                                        const Real rk = cpml[i];
+                                        out = O::fma(Ca, ez, O::mul(O::mul(Cb, O::sub(dHy, dHx)), rk));
+                                        out = O::fma(O::mul(Cb, dxr), ps, out);
+                                    }
+                                    if (iye >= 0) {
+                                        const int ysx = (m <= nc) ? m - 1 : m - (ny - nc) + nc;
+                                        Real ps = O::fma(cpml[nc + iye], psi_in(k, 3, m, c), O::mul(cpml[2 * nc + iye], dHx));
+                                        psi_out(k, 3, m, c, ps, psy_e + (size_t)ysx * (nx + 1) + x);
+                                        const Real rk = cpml[iye];
+                                        out = O::fma(Ca, ez, O::mul(O::mul(Cb, O::sub(dHy, dHx)), rk));
+                                        out = O::fma(-O::mul(Cb, dxr), ps, out);
+                                    }
+                                } else {
+                                    Real cx = dHy, cy = dHx, qx = Real(0), qy = Real(0);
+                                    if (ixe[c] >= 0) {
+                                        const int i = ixe[c];
+                                        const int xsx = (x <= nc) ? x - 1 : x - (nx - nc) + nc;
+                                        qx = O::fma(cpml[nc + i], psi_in(k, 1, m, c), O::mul(cpml[2 * nc + i], dHy));
+                                        psi_out(k, 1, m, c, qx, psx_e + (size_t)m * 2 * nc + xsx);
+                                        cx = O::mul(dHy, cpml[i]);
+                                    }
+                                    if (iye >= 0) {
+                                        const int ysx = (m <= nc) ? m - 1 : m - (ny - nc) + nc;
+                                        qy = O::fma(cpml[nc + iye], psi_in(k, 3, m, c), O::mul(cpml[2 * nc + iye], dHx));
+                                        psi_out(k, 3, m, c, qy, psy_e + (size_t)ysx * (nx + 1) + x);
+                                        cy = O::mul(dHx, cpml[iye]);
+                                    }
+                                    // proper CPML: both stretched derivatives and both psi terms
+                                    if (ixe[c] >= 0 || iye >= 0)
+                                        out = O::fma(Ca, ez, O::mul(Cb, O::fma(dxr, O::sub(qx, qy), O::sub(cx, cy))));
+                                    else
+                                        out = O::fma(Ca, ez, O::mul(Cb, O::sub(dHy, dHx)));
+                                    out = O::fma(-Cj, jp, out);
+                                    if (psrc && m == src_y && x == src_x) out = O::fma(cf[kCs], D.src_wave[n], out);
+                                    jpo = O::fma(Kp, jp, O::mul(Bp, O::sub(out, ez)));
+                                }
+                                if (clampnan && dev_isnan(out)) out = Real(0);
+                                // receivers (owned cells only, so each sample is written once)
+                                if ((mb & kMatRx) && owned[c] && m >= y0 && m < y1) {
+                                    for (int rr = 0; rr < D.nrx; ++rr)
+                                        if (D.rx[2 * rr] == x && D.rx[2 * rr + 1] == m)
+                                            D.traces[(size_t)rr * S + n] = out;
+                                }
+                            }
+                            oz[c] = out;
+                            oj[c] = jpo;
+                        }
+                        // running DFT on the NTFF contour
+                        if (nfreq > 0) {
+                            const Real* ph = phasor + (size_t)n * nfreq * 4;
+                            // horizontal faces: face row m-1 is complete at this level
+                            if ((m - 1 == fd || m - 1 == ny - fd - 1) && m - 1 >= y0 && m - 1 < y1) {
+                                const bool yp = (m - 1 == ny - fd - 1);
+#pragma unroll
+                                for (int c = 0; c < COLS; ++c) {
+                                    const int x = xcol[c];
+                                    if (owned[c] && x >= fd + 1 && x <= nx - fd - 2) {
+                                        Real e = O::mul(O::add(ezn[k][c], oz[c]), Real(0.5));
+                                        Real h = hxn[k][c];
+                                        int ci = yp ? contour_index_yp(nx, ny, fd, x) : contour_index_yn(nx, ny, fd, x);
+                                        if (yp) { e = -e; h = -h; }
+                                        dft_update(acc, ph, nfreq, C, ci, h, e);
+                                    }
+                                }
+                            }
+                            // vertical faces: buffer (h, e) samples per row for a warp-wide flush
+                            if ((has_face0 || has_face1) && m >= fd && m <= ny - fd - 1) {
+                                Real ezR2_last = __shfl_down_sync(0xffffffffu, oz[0], 1);
+#pragma unroll
+                                for (int c = 0; c < COLS; ++c) {
+                                    if (face_slot[c] >= 0) {
+                                        Real ezR2 = (c + 1 < COLS) ? oz[c + 1] : ezR2_last;
+                                        Real e = O::mul(O::add(oz[c], ezR2), Real(0.5));
+                                        Real* s = ws.ring[face_slot[c]][m % kRing][k];
+                                        s[0] = oy[c];
+                                        s[1] = e;
+                                    }
+                                }
+                            }
+                        }
+                    } else {
+                        // beyond the last time step: pass through unchanged (psi included)
+#pragma unroll
+                        for (int c = 0; c < COLS; ++c) {
+                            oz[c] = pz[k][c]; ox[c] = px_[k][c]; oy[c] = py_[k][c]; oj[c] = pj[k][c];
+                            const int x = xcol[c];
+                            if (ixh[c] >= 0 && m < ny) {
+                                const int xsx = (x < nc) ? x : x - (nx - nc) + nc;
+                                psi_out(k, 0, m, c, psi_in(k, 0, m, c), psx_h + (size_t)m * 2 * nc + xsx);
+                            }
+                            if (ixe[c] >= 0 && m >= 1 && m <= ny - 1) {
+                                const int xsx = (x <= nc) ? x - 1 : x - (nx - nc) + nc;
+                                psi_out(k, 1, m, c, psi_in(k, 1, m, c), psx_e + (size_t)m * 2 * nc + xsx);
+                            }
+                            if (x >= 0 && x <= nx) {
+                                const int iyh = (m < nc) ? m : ((m >= ny - nc && m < ny) ? m - (ny - nc) + nc : -1);
+                                if (iyh >= 0 && x < nx)
+                                    psi_out(k, 2, m, c, psi_in(k, 2, m, c), psy_h + (size_t)iyh * (nx + 1) + x);
+                                const int iye = (m >= 1 && m <= nc) ? m - 1
+                                                : ((m >= ny - nc && m <= ny - 1) ? m - (ny - nc) + nc : -1);
+                                if (iye >= 0 && x >= 1 && x <= nx - 1)
+                                    psi_out(k, 3, m, c, psi_in(k, 3, m, c), psy_e + (size_t)iye * (nx + 1) + x);
+                            }
+                        }
+                    }
+                    // ---- emit row m
+#pragma unroll
+                    for (int c = 0; c < COLS; ++c) {
+                        hxn[k][c] = ox[c];
+                        ezn[k][c] = oz[c];
+                    }
+                    if (k + 1 < T) {
+                        hmat[k + 1] = pmat[k];
+#pragma unroll
+                        for (int c = 0; c < COLS; ++c) {
+                            hz[k + 1][c] = oz[c]; hxr[k + 1][c] = ox[c]; hyr[k + 1][c] = oy[c]; hj[k + 1][c] = oj[c];
+                        }
+                    } else if (m >= y0 && m < y1) {   // owned rows only
+                        const long long rowoff = (long long)m * pitch;
+                        const bool jrow = m >= jy0 && m <= jy1;
+#pragma unroll
+                        for (int c = 0; c < COLS; ++c) {
+                            if (owned[c]) {
+                                const int x = xcol[c];
+                                ez_d[rowoff + x] = oz[c];
+                                hx_d[rowoff + x] = ox[c];
+                                hy_d[rowoff + x] = oy[c];
+                                if (jrow && x >= jx0 && x <= jx1) jp_d[rowoff + x] = oj[c];
+                            }
+                        }
+                    }
+                }
+                // the received row becomes this level's previous row
+                pmat[k] = im;
+#pragma unroll
+                for (int c = 0; c < COLS; ++c) {
+                    pz[k][c] = iz[c]; px_[k][c] = ix[c]; py_[k][c] = iy[c]; pj[k][c] = ij[c];
+                }
             }
         }
 
