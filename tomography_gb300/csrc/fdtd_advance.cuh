@@ -419,6 +419,19 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
             const int m = r - 2 * k - 1;
             interior = interior && k < nsteps && m > nc && m < ny - nc && !((rowbits[m >> 5] >> (m & 31)) & 1u);
         }
+        // the same for the narrow edge strips (breast mode): every level on the edge
+        // path, off the y-CPML rows and inside the vertical NTFF faces' row range
+        bool edge_rows = false;
+        if constexpr (kEdgePath) {
+            edge_rows = wspecial;
+#pragma unroll
+            for (int k = 0; k < T; ++k) {
+                const int m = r - 2 * k - 1;
+                edge_rows = edge_rows && k < nsteps && m > nc && m < ny - nc &&
+                            (!(has_face0 || has_face1) || (m >= fd && m <= ny - fd - 1)) &&
+                            !((rowbits[m >> 5] >> (m & 31)) & 1u);
+            }
+        }
         if (interior) {
 #pragma unroll
             for (int k = T - 1; k >= 0; --k) {
@@ -460,6 +473,113 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
                     oj[c] = O::fma(Kp, jp, O::mul(Bp, O::sub(out, ez)));
                     if (clampnan && dev_isnan(out)) out = Real(0);
                     oz[c] = out;
+                }
+#pragma unroll
+                for (int c = 0; c < COLS; ++c) {
+                    hxn[k][c] = ox[c];
+                    ezn[k][c] = oz[c];
+                }
+                if (k + 1 < T) {
+                    hmat[k + 1] = pmat[k];
+#pragma unroll
+                    for (int c = 0; c < COLS; ++c) {
+                        hz[k + 1][c] = oz[c]; hxr[k + 1][c] = ox[c]; hyr[k + 1][c] = oy[c]; hj[k + 1][c] = oj[c];
+                    }
+                } else if (m >= y0 && m < y1) {   // owned rows only
+                    const long long rowoff = (long long)m * pitch;
+                    const bool jrow = m >= jy0 && m <= jy1;
+#pragma unroll
+                    for (int c = 0; c < COLS; ++c) {
+                        if (owned[c]) {
+                            const int x = xcol[c];
+                            ez_d[rowoff + x] = oz[c];
+                            hx_d[rowoff + x] = ox[c];
+                            hy_d[rowoff + x] = oy[c];
+                            if (jrow && x >= jx0 && x <= jx1) jp_d[rowoff + x] = oj[c];
+                        }
+                    }
+                }
+                pmat[k] = im;
+#pragma unroll
+                for (int c = 0; c < COLS; ++c) {
+                    pz[k][c] = iz[c]; px_[k][c] = ix[c]; py_[k][c] = iy[c]; pj[k][c] = ij[c];
+                }
+            }
+        } else if (edge_rows) {
+#pragma unroll
+            for (int k = T - 1; k >= 0; --k) {
+                const int m = r - 2 * k - 1;
+                Real iz[COLS], ix[COLS], iy[COLS], ij[COLS];
+                const uint32_t im = (k == 0) ? lm : hmat[k];
+#pragma unroll
+                for (int c = 0; c < COLS; ++c) {
+                    if (k == 0) { iz[c] = lz[c]; ix[c] = lx[c]; iy[c] = ly[c]; ij[c] = lj[c]; }
+                    else { iz[c] = hz[k][c]; ix[c] = hxr[k][c]; iy[c] = hyr[k][c]; ij[c] = hj[k][c]; }
+                }
+                Real oz[COLS], ox[COLS], oy[COLS], oj[COLS];
+                const Real ezR_last = __shfl_down_sync(0xffffffffu, pz[k][0], 1);
+#pragma unroll
+                for (int c = 0; c < COLS; ++c) {
+                    const int x = xcol[c];
+                    const bool hin = x >= 0 && x < nx;
+                    const bool isx = ixh[c] >= 0;
+                    const int i = isx ? ixh[c] : 0;
+                    const Real ez0 = pz[k][c];
+                    const Real ezR = (c + 1 < COLS) ? pz[k][c + 1] : ezR_last;
+                    const Real hx0 = px_[k][c], hy0 = py_[k][c];
+                    const Real dEy = O::sub(ezR, ez0);
+                    const Real dEx = O::sub(iz[c], ez0);
+                    const Real hy = O::fma(chez, dEy, hy0);
+                    const Real hx = O::fma(-chez, dEx, hx0);
+                    const Real psx = O::fma(cpml[4 * nc + i], psi_in(k, 0, m, c), O::mul(cpml[5 * nc + i], dEy));
+                    Real hyc = O::fma(O::mul(chez, dEy), cpml[3 * nc + i], hy0);
+                    hyc = O::fma(O::mul(chez, dxr), psx, hyc);
+                    if (isx) {
+                        const int xsx = (x < nc) ? x : x - (nx - nc) + nc;
+                        psi_out(k, 0, m, c, psx, psx_h + (size_t)m * 2 * nc + xsx);
+                    }
+                    ox[c] = hin ? hx : hx0;
+                    oy[c] = hin ? (isx ? hyc : hy) : hy0;
+                }
+                const Real hyL_first = __shfl_up_sync(0xffffffffu, oy[COLS - 1], 1);
+#pragma unroll
+                for (int c = 0; c < COLS; ++c) {
+                    const int x = xcol[c];
+                    const bool ein = x >= 1 && x <= nx - 1;
+                    const bool isx = ixe[c] >= 0;
+                    const int i = isx ? ixe[c] : 0;
+                    const int mi = (pmat[k] >> (8 * c)) & kMatMask;
+                    Real Ca, Cb, Cj, Bp;
+                    load_coefs(ws.tab[mi], Ca, Cb, Cj, Bp);
+                    const Real hyL = (c > 0) ? oy[c - 1] : hyL_first;
+                    const Real dHy = O::sub(oy[c], hyL);
+                    const Real dHx = O::sub(ox[c], hxn[k][c]);
+                    const Real ez = pz[k][c], jp = pj[k][c];
+                    const Real qxc = O::fma(cpml[nc + i], psi_in(k, 1, m, c), O::mul(cpml[2 * nc + i], dHy));
+                    if (isx) {
+                        const int xsx = (x <= nc) ? x - 1 : x - (nx - nc) + nc;
+                        psi_out(k, 1, m, c, qxc, psx_e + (size_t)m * 2 * nc + xsx);
+                    }
+                    const Real cxc = O::mul(dHy, cpml[i]);
+                    const Real outc = O::fma(Ca, ez, O::mul(Cb, O::fma(dxr, O::sub(qxc, Real(0)), O::sub(cxc, dHx))));
+                    const Real outp = O::fma(Ca, ez, O::mul(Cb, O::sub(dHy, dHx)));
+                    Real out = isx ? outc : outp;
+                    out = O::fma(-Cj, jp, out);
+                    const Real jpo = O::fma(Kp, jp, O::mul(Bp, O::sub(out, ez)));
+                    oz[c] = ein ? out : Real(0);
+                    oj[c] = ein ? jpo : jp;
+                }
+                if (has_face0 || has_face1) {
+                    const Real ezR2_last = __shfl_down_sync(0xffffffffu, oz[0], 1);
+#pragma unroll
+                    for (int c = 0; c < COLS; ++c) {
+                        if (face_slot[c] >= 0) {
+                            const Real ezR2 = (c + 1 < COLS) ? oz[c + 1] : ezR2_last;
+                            Real* smp = ws.ring[face_slot[c]][m % kRing][k];
+                            smp[0] = oy[c];
+                            smp[1] = O::mul(O::add(oz[c], ezR2), Real(0.5));
+                        }
+                    }
                 }
 #pragma unroll
                 for (int c = 0; c < COLS; ++c) {
