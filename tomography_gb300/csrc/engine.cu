@@ -344,8 +344,10 @@ SolveLayout solve_layout(const ProblemClass& pc, size_t real_bytes) {
     L.tr_stride = std::max<size_t>((size_t)pc.nrx * pc.S, 1);
     L.tr_stride = (L.tr_stride + 31) / 32 * 32;
     L.acc_stride = std::max<size_t>((size_t)pc.nfreq * pc.C * 8, 8);
+    L.acc_stride = (L.acc_stride + 31) / 32 * 32;
     const int tmax = 8;
-    L.per_solve = 8 * L.field_elems + (size_t)(tmax + 1) * L.psi_elems + L.tr_stride + L.acc_stride;
+    L.stage_stride = pc.nfreq > 0 ? ((size_t)tmax * pc.C * 2 + 31) / 32 * 32 : 32;
+    L.per_solve = 8 * L.field_elems + (size_t)(tmax + 1) * L.psi_elems + L.tr_stride + L.acc_stride + L.stage_stride;
     L.per_solve = (L.per_solve + 63) / 64 * 64;
     L.mat_stride = rows * pc.mpitch;
     (void)real_bytes;
@@ -529,11 +531,11 @@ int EngineT<Real>::autotune(size_t ncand) {
         TOMO_TRY(advance_grid<Real>(c, mode, (int)items.size(), num_sms_, &blocks, &smem));
         const int L = std::max(2, kTuneSteps / c.T);
         launch_advance<Real>(c, mode, blocks, smem, d_descs_.as<SolveDesc<Real>>(), d_tune_items_.as<WorkItem>(),
-                             (int)items.size(), nsolves, d_counter_.as<int>(), stream_);
+                             (int)items.size(), nsolves, d_counter_.as<int>(), dft_contour(pc), stream_);
         CUDA_TRY(cudaEventRecord(ev_[1], stream_));
         for (int l = 0; l < L; ++l)
             launch_advance<Real>(c, mode, blocks, smem, d_descs_.as<SolveDesc<Real>>(), d_tune_items_.as<WorkItem>(),
-                                 (int)items.size(), nsolves, d_counter_.as<int>(), stream_);
+                                 (int)items.size(), nsolves, d_counter_.as<int>(), dft_contour(pc), stream_);
         CUDA_TRY(cudaEventRecord(ev_[2], stream_));
         CUDA_TRY(cudaStreamSynchronize(stream_));
         CUDA_TRY(cudaGetLastError());
@@ -631,7 +633,8 @@ int EngineT<Real>::build_graph(int nlaunch) {
     CUDA_TRY(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
     for (int l = 0; l < nlaunch; ++l)
         launch_advance<Real>(blk_, advance_mode(cd_.pc.spec), blocks, smem, d_descs_.as<SolveDesc<Real>>(),
-                             d_items_.as<WorkItem>(), nitems_, nsolves_, d_counter_.as<int>(), stream_);
+                             d_items_.as<WorkItem>(), nitems_, nsolves_, d_counter_.as<int>(), dft_contour(cd_.pc),
+                             stream_);
     cudaError_t ce = cudaStreamEndCapture(stream_, &graph);
     if (ce != cudaSuccess) return fail(TOMO_ECUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
     ce = cudaGraphInstantiate(&graph_exec_, graph, 0);
@@ -697,7 +700,7 @@ int EngineT<Real>::forward(const double* args, size_t ncand, size_t nparam, cons
         CUDA_TRY(cudaEventRecord(ev_[1], stream_));
         CUDA_TRY(cudaGraphLaunch(graph_exec_, stream_));
         CUDA_TRY(cudaEventRecord(ev_[2], stream_));
-        kernels += 2 * (int64_t)nlaunch;
+        kernels += (dft_contour(pc) > 0 ? 3 : 2) * (int64_t)nlaunch;
     }
 
     CUDA_TRY(cudaMemsetAsync(d_flag_.p, 0, sizeof(int) * 4, stream_));

@@ -89,7 +89,7 @@ bool same_problem(const tomo_spec& a, const tomo_spec& b);
 
 // Per-solve memory layout (elements of Real), identical for every solve of a class.
 struct SolveLayout {
-    size_t field_elems, psi_elems, tr_stride, acc_stride, per_solve, mat_stride;
+    size_t field_elems, psi_elems, tr_stride, acc_stride, stage_stride, per_solve, mat_stride;
 };
 SolveLayout solve_layout(const ProblemClass& pc, size_t real_bytes);
 
@@ -229,6 +229,7 @@ void fill_descs(const ClassData<Real>& cd, const Unpacked& u, Real* state_base, 
         D.psi_stride = (int)L.psi_elems;
         D.traces = psib + (size_t)9 * L.psi_elems;
         D.acc = D.traces + L.tr_stride;
+        D.stage = D.acc + L.acc_stride;
         D.mtab = tabs + (size_t)cand * kMaxMat * kMatCoef;
         D.cpml = cd.cpml.template as<Real>();
         D.src_wave = cd.wave.template as<Real>();
@@ -340,14 +341,23 @@ std::vector<Blocking> tune_candidates(int mode, int fixT, int fixCols, int fixMi
 template <typename Real>
 int launch_plain_step(int mode, const SolveDesc<Real>* d, int n, int nx, int ny, int n_contour, cudaStream_t st);
 
+// One advance launch (T steps of every listed solve), then the running DFT of
+// the contours staged by it (when cmax, the largest contour among the solves,
+// is positive), then the progress bump.  Returns the number of kernels.
 template <typename Real>
-void launch_advance(const Blocking& b, int mode, int blocks, size_t smem, const SolveDesc<Real>* descs,
-                    const WorkItem* items, int nitems, int nsolves, int* counter, cudaStream_t st) {
+int launch_advance(const Blocking& b, int mode, int blocks, size_t smem, const SolveDesc<Real>* descs,
+                   const WorkItem* items, int nitems, int nsolves, int* counter, int cmax, cudaStream_t st) {
     AdvanceFn<Real> fn = advance_kernel_for<Real>(b, mode);
     fn<<<blocks, 128, smem, st>>>(descs, items, nitems, counter);
+    if (cmax > 0)
+        dft_accumulate_kernel<Real><<<dim3(nsolves, (cmax + 127) / 128), 128, 0, st>>>(descs, b.T);
     bump_kernel<Real><<<(nsolves + 127) / 128, 128, 0, st>>>(const_cast<SolveDesc<Real>*>(descs), nsolves, b.T,
                                                             counter);
+    return cmax > 0 ? 3 : 2;
 }
+
+// Largest NTFF contour of a class as launch_advance wants it (0: no NTFF).
+inline int dft_contour(const ProblemClass& pc) { return pc.nfreq > 0 ? pc.C : 0; }
 
 // Work items of nsolves solves of a grid with nx + 1 columns, starting at
 // solve index `first`.  Columns x <= lo and x >= hi (PEC boundary, CPML,

@@ -158,6 +158,34 @@ __device__ __forceinline__ void dft_update(Real* acc, const Real* ph, int nfreq,
     }
 }
 
+// Running DFT of the NTFF contour (FDTD_GPU.cu:231-280) for the time steps the
+// last advance launch computed: one thread per (solve, contour point) adds the
+// staged (h, e) samples of the launch's levels in time order, with the same
+// compensated sums as one update per step.  Runs between the advance launch
+// and the progress bump (which moves `step`).
+template <typename Real>
+__global__ void __launch_bounds__(128) dft_accumulate_kernel(const SolveDesc<Real>* __restrict__ descs, int T) {
+    const SolveDesc<Real>& D = descs[blockIdx.x];
+    const int c = blockIdx.y * blockDim.x + threadIdx.x;
+    const int C = D.n_contour, nfreq = D.nfreq;
+    if (!D.active || nfreq <= 0 || c >= C) return;
+    const int n0 = D.step, nsteps = min(T, D.steps_total - n0);
+    for (int f = 0; f < nfreq; ++f) {
+        Real* a = D.acc + ((size_t)f * C + c) * 8;
+        Real s0 = a[0], s1 = a[1], c0 = a[2], c1 = a[3], s2 = a[4], s3 = a[5], c2 = a[6], c3 = a[7];
+        for (int k = 0; k < nsteps; ++k) {
+            const Real* p = D.phasor + ((size_t)(n0 + k) * nfreq + f) * 4;
+            const Real* sp = D.stage + ((size_t)k * C + c) * 2;
+            const Real h = sp[0], e = sp[1];
+            acc_add(s0, c0, Op<Real>::mul(h, p[0]));
+            acc_add(s1, c1, Op<Real>::mul(h, p[1]));
+            acc_add(s2, c2, Op<Real>::mul(e, p[2]));
+            acc_add(s3, c3, Op<Real>::mul(e, p[3]));
+        }
+        a[0] = s0; a[1] = s1; a[2] = c0; a[3] = c1; a[4] = s2; a[5] = s3; a[6] = c2; a[7] = c3;
+    }
+}
+
 // Ca, Cb, Cj, Bp of one material from the per-warp table (one 16-byte load in FP32).
 __device__ __forceinline__ void load_coefs(const float* t, float& a, float& b, float& c, float& d) {
     const float4 v = *reinterpret_cast<const float4*>(t);
@@ -177,7 +205,6 @@ struct WarpSmem {
     Real pslev[T > 1 ? T - 1 : 1][4][4][32 * COLS];   // psi after level k, 4 rows in flight
     Real tab[kMaxMat][4];                 // Ca, Cb, Cj, Bp of every material
     Real cpml[6 * kMaxCpml];              // CPML profile (1/ke, be, ae, 1/km, bm, am)
-    Real ring[2][kRing][T][2];            // vertical-face DFT samples (h, e)
     uint32_t rowbits[kMaxRowWords];       // "row needs the general path" flags
     uint8_t mats[kRowSlots][32 * COLS + 16];   // prefetch ring: material bytes
 };
@@ -222,8 +249,7 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
     const int psy_h = psy0, psy_e = psy0 + 2 * nc * (nx + 1);         // y-strip psi sub-arrays
     const uint8_t* __restrict__ matp = D.mat;
     Real* const cpml = ws.cpml;   // CPML profile, copied to shared memory below
-    const Real* __restrict__ phasor = D.phasor;
-    Real* __restrict__ acc = D.acc;
+    Real* __restrict__ stage = D.stage;   // [T][C][2] contour samples of this launch's levels
     const int mpitch = D.mpitch, jx0 = D.jx0, jx1 = D.jx1, jy0 = D.jy0, jy1 = D.jy1;
     const int src_x = D.src_x, src_y = D.src_y;
 
@@ -329,6 +355,17 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
         if (k + 1 < T) ws.pslev[k % (T > 1 ? T - 1 : 1)][f][m & 3][lane * COLS + c] = v;
         else if (owned[c] && m >= y0 && m < y1) psi_dst[goff] = v;
     };
+    // vertical NTFF faces: stage the (h, e) sample of an owned face cell of row m
+    // at level k (outward normal -x on the left face, +x on the right face)
+    auto stage_vertical = [&](int k, int m, int c, Real h, Real e) {
+        if (face_slot[c] >= 0 && m >= y0 && m < y1) {
+            const int ci = face_slot[c] == 0 ? contour_index_xn(nx, ny, fd, m) : contour_index_xp(nx, ny, fd, m);
+            const Real sg = face_slot[c] == 0 ? Real(-1) : Real(1);
+            Real* sp = stage + ((size_t)k * C + ci) * 2;
+            sp[0] = sg * h;
+            sp[1] = sg * e;
+        }
+    };
     bool wxs = false;   // warp holds an x-strip column (uniform)
 #pragma unroll
     for (int c = 0; c < COLS; ++c) wxs |= ixh[c] >= 0 || ixe[c] >= 0;
@@ -390,7 +427,6 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
 #pragma unroll 1
     for (int r = rstart; r < rstart + kPrefetch; ++r) issue_row(r);
 
-    int flushed = y0;   // next face row not yet flushed
     for (int r = rstart; r <= rmax; ++r) {
         // ---- level 0 input: row r from the ring; request row r + kPrefetch
         cp_async_wait<kPrefetch - 1>();
@@ -573,12 +609,8 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
                     const Real ezR2_last = __shfl_down_sync(0xffffffffu, oz[0], 1);
 #pragma unroll
                     for (int c = 0; c < COLS; ++c) {
-                        if (face_slot[c] >= 0) {
-                            const Real ezR2 = (c + 1 < COLS) ? oz[c + 1] : ezR2_last;
-                            Real* smp = ws.ring[face_slot[c]][m % kRing][k];
-                            smp[0] = oy[c];
-                            smp[1] = O::mul(O::add(oz[c], ezR2), Real(0.5));
-                        }
+                        const Real ezR2 = (c + 1 < COLS) ? oz[c + 1] : ezR2_last;
+                        stage_vertical(k, m, c, oy[c], O::mul(O::add(oz[c], ezR2), Real(0.5)));
                     }
                 }
 #pragma unroll
@@ -763,17 +795,13 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
                             oz[c] = ein ? out : Real(0);
                             oj[c] = ein ? jpo : jp;
                         }
-                        // vertical NTFF faces: buffer (h, e) samples for the warp-wide flush
+                        // vertical NTFF faces: stage this level's (h, e) samples
                         if (nfreq > 0 && (has_face0 || has_face1) && m >= fd && m <= ny - fd - 1) {
                             const Real ezR2_last = __shfl_down_sync(0xffffffffu, oz[0], 1);
 #pragma unroll
                             for (int c = 0; c < COLS; ++c) {
-                                if (face_slot[c] >= 0) {
-                                    const Real ezR2 = (c + 1 < COLS) ? oz[c + 1] : ezR2_last;
-                                    Real* smp = ws.ring[face_slot[c]][m % kRing][k];
-                                    smp[0] = oy[c];
-                                    smp[1] = O::mul(O::add(oz[c], ezR2), Real(0.5));
-                                }
+                                const Real ezR2 = (c + 1 < COLS) ? oz[c + 1] : ezR2_last;
+                                stage_vertical(k, m, c, oy[c], O::mul(O::add(oz[c], ezR2), Real(0.5)));
                             }
                         }
                     } else if (k < nsteps) {
@@ -907,9 +935,8 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
                             oz[c] = out;
                             oj[c] = jpo;
                         }
-                        // running DFT on the NTFF contour
+                        // NTFF contour samples of this level, summed by the DFT kernel
                         if (nfreq > 0) {
-                            const Real* ph = phasor + (size_t)n * nfreq * 4;
                             // horizontal faces: face row m-1 is complete at this level
                             if ((m - 1 == fd || m - 1 == ny - fd - 1) && m - 1 >= y0 && m - 1 < y1) {
                                 const bool yp = (m - 1 == ny - fd - 1);
@@ -921,22 +948,19 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
                                         Real h = hxn[k][c];
                                         int ci = yp ? contour_index_yp(nx, ny, fd, x) : contour_index_yn(nx, ny, fd, x);
                                         if (yp) { e = -e; h = -h; }
-                                        dft_update(acc, ph, nfreq, C, ci, h, e);
+                                        Real* sp = stage + ((size_t)k * C + ci) * 2;
+                                        sp[0] = h;
+                                        sp[1] = e;
                                     }
                                 }
                             }
-                            // vertical faces: buffer (h, e) samples per row for a warp-wide flush
+                            // vertical faces
                             if ((has_face0 || has_face1) && m >= fd && m <= ny - fd - 1) {
-                                Real ezR2_last = __shfl_down_sync(0xffffffffu, oz[0], 1);
+                                const Real ezR2_last = __shfl_down_sync(0xffffffffu, oz[0], 1);
 #pragma unroll
                                 for (int c = 0; c < COLS; ++c) {
-                                    if (face_slot[c] >= 0) {
-                                        Real ezR2 = (c + 1 < COLS) ? oz[c + 1] : ezR2_last;
-                                        Real e = O::mul(O::add(oz[c], ezR2), Real(0.5));
-                                        Real* s = ws.ring[face_slot[c]][m % kRing][k];
-                                        s[0] = oy[c];
-                                        s[1] = e;
-                                    }
+                                    const Real ezR2 = (c + 1 < COLS) ? oz[c + 1] : ezR2_last;
+                                    stage_vertical(k, m, c, oy[c], O::mul(O::add(oz[c], ezR2), Real(0.5)));
                                 }
                             }
                         }
@@ -1001,44 +1025,6 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
             }
         }
 
-        // ---- vertical-face DFT flush: rows whose T levels are all done
-        if (has_face0 || has_face1) {
-            const int done = r - 2 * T + 1;   // last row completed by level T-1
-            const bool last = (r == rmax);
-            if (last || ((done + 1 - flushed) >= 32)) {
-                __syncwarp();
-                const int upto = min(last ? ny : done, y1 - 1);
-                while (flushed <= upto) {
-                    const int m = flushed + lane;
-                    if (m <= upto && m >= fd && m <= ny - fd - 1) {
-                        for (int face = 0; face < 2; ++face) {
-                            if (!(face == 0 ? has_face0 : has_face1)) continue;
-                            const int ci = face == 0 ? contour_index_xn(nx, ny, fd, m) : contour_index_xp(nx, ny, fd, m);
-                            const Real sgn = face == 0 ? Real(-1) : Real(1);
-                            for (int f = 0; f < nfreq; ++f) {
-                                Real* a = acc + ((size_t)f * C + ci) * 8;
-                                Real s0 = a[0], s1 = a[1], c0 = a[2], c1 = a[3], s2 = a[4], s3 = a[5], c2 = a[6],
-                                     c3 = a[7];
-                                for (int k = 0; k < nsteps; ++k) {
-                                    const Real* p = phasor + ((size_t)(n0 + k) * nfreq + f) * 4;
-                                    const Real* sm_s = ws.ring[face][m % kRing][k];
-                                    Real h = sgn * sm_s[0], e = sgn * sm_s[1];
-                                    acc_add(s0, c0, Op<Real>::mul(h, p[0]));
-                                    acc_add(s1, c1, Op<Real>::mul(h, p[1]));
-                                    acc_add(s2, c2, Op<Real>::mul(e, p[2]));
-                                    acc_add(s3, c3, Op<Real>::mul(e, p[3]));
-                                }
-                                a[0] = s0; a[1] = s1; a[2] = c0; a[3] = c1;
-                                a[4] = s2; a[5] = s3; a[6] = c2; a[7] = c3;
-                            }
-                        }
-                    }
-                    flushed += 32;
-                }
-                if (flushed > upto + 1) flushed = upto + 1;
-                __syncwarp();
-            }
-        }
         // request row r + kPrefetch into the slot of row r - 1 (no longer read)
         __syncwarp();
         issue_row(r + kPrefetch);

@@ -73,6 +73,7 @@ struct ServeStateT {
     size_t smem = 0;
     int hi_slot = 0;   // one past the highest slot ever used
     Blocking blk{0, 0, 0};   // blocking of the serving loop, fixed at the first serving step
+    int cmax = 0;             // largest NTFF contour among the running requests
 
     int find_range(int n) {
         int run = 0;
@@ -303,6 +304,7 @@ int EngineT<Real>::serve_step(int* n_active) {
             nymax = std::max(nymax, pc.ny);
         }
         const int nseg = choose_segments(strips, nymax, st->blk.T, 24L * num_sms_);
+        st->cmax = 0;
         for (auto& kv : st->reqs) {
             const ServeRequest<Real>& r = *kv.second;
             if (r.state != kRunning) continue;
@@ -311,6 +313,7 @@ int EngineT<Real>::serve_step(int* n_active) {
             append_items(items, r.first, r.nsolves, pc.nx, pc.ny, pc.nc, item_face_distance(pc), st->blk.T,
                          st->blk.cols, nseg);
             TOMO_TRY(validate_items(items, n0, pc.nx, pc.ny, st->blk.T, st->blk.cols));
+            st->cmax = std::max(st->cmax, dft_contour(pc));
         }
         st->nitems = (int)items.size();
         if (!items.empty()) {
@@ -341,7 +344,7 @@ int EngineT<Real>::serve_step(int* n_active) {
         for (int l = 0; l < nl; ++l)
             launch_advance<Real>(st->blk, advance_mode(cd_.pc.spec), st->blocks, st->smem,
                                  st->descs.template as<SolveDesc<Real>>(), st->items.template as<WorkItem>(),
-                                 st->nitems, st->hi_slot, d_counter_.as<int>(), stream_);
+                                 st->nitems, st->hi_slot, d_counter_.as<int>(), st->cmax, stream_);
         CUDA_TRY(cudaGetLastError());
         for (auto& kv : st->reqs) {
             ServeRequest<Real>& r = *kv.second;

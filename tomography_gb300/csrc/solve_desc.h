@@ -25,7 +25,6 @@ constexpr int kMaxMat = 128;     // material indices per solve (7 bits)
 constexpr int kMatCoef = 8;      // coefficient columns, see MatCol
 constexpr int kMaxRx = 64;
 constexpr int kMaxCpml = 32;     // CPML cells per side (the profile lives in shared memory)
-constexpr int kRing = 64;        // rows buffered for vertical-face DFT samples
 
 enum SolveFlags : int {
     kRefCpml = 1,     // reference E-update strip semantics (FDTD_GPU.cu:389-416)
@@ -72,6 +71,8 @@ struct SolveDesc {
     Real* traces;                // [nrx][steps_total]
     const Real* phasor;          // [steps_total][nfreq][4]: dt*exp(-jwn dt), dt*exp(-jw(n+1/2)dt)
     Real* acc;                   // [nfreq][n_contour][8]: J sum re/im, J comp re/im, M sum, M comp
+    Real* stage;                 // [T][n_contour][2]: (h, e) contour samples of the levels of the last
+                                 // advance launch, summed into acc by the DFT kernel
     // plane wave (reference modes): g = exp(-(ar/tau)^2),
     // ar = (t dt - t0 + l/c0) - (ky (y - yoff) + kx (x - xoff)) dx/c0
     double pw_kx, pw_ky, pw_xoff, pw_yoff, pw_t0l, pw_inv_tau, pw_dxc0, dt;
