@@ -163,6 +163,34 @@ __device__ __forceinline__ void dft_update(Real* acc, const Real* ph, int nfreq,
 // staged (h, e) samples of the launch's levels in time order, with the same
 // compensated sums as one update per step.  Runs between the advance launch
 // and the progress bump (which moves `step`).
+// Accumulators of one (frequency, contour point) and a phasor as vectors
+// (32 and 16 bytes, aligned: the accumulator and phasor arrays start on
+// 128-byte boundaries and hold 8 and 4 values per entry).
+template <typename Real>
+struct Vec4;
+template <>
+struct Vec4<float> {
+    using type = float4;
+    static __device__ __forceinline__ void load(const float* p, float (&v)[4]) {
+        const float4 x = *reinterpret_cast<const float4*>(p);
+        v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+    }
+    static __device__ __forceinline__ void store(float* p, const float (&v)[4]) {
+        *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    }
+};
+template <>
+struct Vec4<double> {
+    static __device__ __forceinline__ void load(const double* p, double (&v)[4]) {
+        const double2 x = reinterpret_cast<const double2*>(p)[0], y = reinterpret_cast<const double2*>(p)[1];
+        v[0] = x.x; v[1] = x.y; v[2] = y.x; v[3] = y.y;
+    }
+    static __device__ __forceinline__ void store(double* p, const double (&v)[4]) {
+        reinterpret_cast<double2*>(p)[0] = make_double2(v[0], v[1]);
+        reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
+    }
+};
+
 template <typename Real>
 __global__ void __launch_bounds__(128) dft_accumulate_kernel(const SolveDesc<Real>* __restrict__ descs, int T) {
     const SolveDesc<Real>& D = descs[blockIdx.x];
@@ -172,17 +200,21 @@ __global__ void __launch_bounds__(128) dft_accumulate_kernel(const SolveDesc<Rea
     const int n0 = D.step, nsteps = min(T, D.steps_total - n0);
     for (int f = 0; f < nfreq; ++f) {
         Real* a = D.acc + ((size_t)f * C + c) * 8;
-        Real s0 = a[0], s1 = a[1], c0 = a[2], c1 = a[3], s2 = a[4], s3 = a[5], c2 = a[6], c3 = a[7];
+        Real j[4], mm[4];   // J: sum re, sum im, comp re, comp im; M likewise
+        Vec4<Real>::load(a, j);
+        Vec4<Real>::load(a + 4, mm);
         for (int k = 0; k < nsteps; ++k) {
-            const Real* p = D.phasor + ((size_t)(n0 + k) * nfreq + f) * 4;
+            Real p[4];
+            Vec4<Real>::load(D.phasor + ((size_t)(n0 + k) * nfreq + f) * 4, p);
             const Real* sp = D.stage + ((size_t)k * C + c) * 2;
             const Real h = sp[0], e = sp[1];
-            acc_add(s0, c0, Op<Real>::mul(h, p[0]));
-            acc_add(s1, c1, Op<Real>::mul(h, p[1]));
-            acc_add(s2, c2, Op<Real>::mul(e, p[2]));
-            acc_add(s3, c3, Op<Real>::mul(e, p[3]));
+            acc_add(j[0], j[2], Op<Real>::mul(h, p[0]));
+            acc_add(j[1], j[3], Op<Real>::mul(h, p[1]));
+            acc_add(mm[0], mm[2], Op<Real>::mul(e, p[2]));
+            acc_add(mm[1], mm[3], Op<Real>::mul(e, p[3]));
         }
-        a[0] = s0; a[1] = s1; a[2] = c0; a[3] = c1; a[4] = s2; a[5] = s3; a[6] = c2; a[7] = c3;
+        Vec4<Real>::store(a, j);
+        Vec4<Real>::store(a + 4, mm);
     }
 }
 
