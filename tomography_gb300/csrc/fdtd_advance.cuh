@@ -299,7 +299,6 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
     for (int c = 0; c < COLS; ++c) {
         int x = xs + lane * COLS + c;
         xcol[c] = x;
-        int pos = lane * COLS + c;
         owned[c] = x >= ox0 && x < ox1;
         ixh[c] = (x >= 0 && x < nc) ? nc - 1 - x : ((x >= nx - nc && x < nx) ? x - nx + nc : -1);
         ixe[c] = (x >= 1 && x <= nc) ? nc - x : ((x >= nx - nc && x <= nx - 1) ? x - nx + nc : -1);
