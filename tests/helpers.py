@@ -5,8 +5,11 @@ import numpy as np
 
 
 def rel_l2(got, want) -> float:
-    got = np.asarray(got, dtype=np.float64)
-    want = np.asarray(want, dtype=np.float64)
+    """Relative L2 error; complex arrays (DFT surface currents) compare both parts."""
+    got, want = np.asarray(got), np.asarray(want)
+    dt = np.complex128 if (np.iscomplexobj(got) or np.iscomplexobj(want)) else np.float64
+    got = got.astype(dt)
+    want = want.astype(dt)
     den = np.linalg.norm(want)
     return float(np.linalg.norm(got - want) / den) if den > 0 else float(np.linalg.norm(got))
 
