@@ -1056,8 +1056,9 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
             }
         }
 
-        // request row r + kPrefetch into the slot of row r - 1 (no longer read)
-        __syncwarp();
+        // request row r + kPrefetch into the slot of row r - 1: every lane read that
+        // slot's material bytes before the warp-wide sync at the top of this
+        // iteration, and its own fields and psi earlier in program order
         issue_row(r + kPrefetch);
     }
     cp_async_wait<0>();   // the ring is reused by the warp's next item
