@@ -33,9 +33,15 @@ std::vector<float> read_target_file(const char* path) {
     size_t got = std::fread(raw.data(), 1, raw.size(), fp);
     std::fclose(fp);
     raw.resize(got);
-    bool text = false;
+    // text when every byte can be part of written numbers (raw float32 data
+    // almost surely holds other bytes), else raw little-endian float32
+    static const char kTextBytes[] = "0123456789+-.eEinfaINFA \t\r\n,";
+    bool text = !raw.empty();
     for (unsigned char c : raw)
-        if (c == ',' || c == '\n' || c == ' ') { text = true; break; }
+        if (c == 0 || !std::strchr(kTextBytes, c)) {
+            text = false;
+            break;
+        }
     if (!text && raw.size() % 4 == 0) {
         v.resize(raw.size() / 4);
         std::memcpy(v.data(), raw.data(), raw.size());
