@@ -188,6 +188,19 @@ int tomo_trace_misfit_static(const float *traces, const float *target, size_t n_
                              size_t n_per_solve, double *fitness, void *stream);
 
 int tomo_get_stats(tomo_handle *h, tomo_stats *stats);
+
+/* ---- field snapshots (headless stand-in for the reference's commented-out
+   GL field view, FDTD_GPU.cu:23-25,418-422) */
+#define TOMO_FIELD_EZ 0   /* (ny+1) x (nx+1) values */
+#define TOMO_FIELD_HX 1   /* ny x nx values */
+#define TOMO_FIELD_HY 2   /* ny x nx values */
+/* Copy the final field `field` of solve (candidate, excitation) of the last
+   tomo_forward / tomo_fitness / tomo_fitness_batch call on this handle into
+   out (row-major, y then x, as float; n = capacity of out).  The state stays
+   on the device until the handle's next batch.  TOMO_ENOTREADY before the
+   first batch. */
+int tomo_field_snapshot(tomo_handle *h, size_t candidate, int excitation, int field, float *out, size_t n);
+
 const char *tomo_last_error(void);
 const char *tomo_version(void);
 

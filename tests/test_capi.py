@@ -105,3 +105,16 @@ def test_workload_generator_is_deterministic():
     assert a.shape == (3, 64) and np.array_equal(a, b)
     t = W.target_phantom(1)
     assert t.shape == (24,) and np.all(t[5::8] == 12.9)
+
+
+def test_save_field_image(tomo, tmp_path):
+    f = np.linspace(-1, 1, 12, dtype=np.float32).reshape(3, 4)
+    tomo.save_field(str(tmp_path / "f.npy"), f)
+    np.testing.assert_array_equal(np.load(tmp_path / "f.npy"), f)
+    tomo.save_field(str(tmp_path / "f.pgm"), f)
+    data = (tmp_path / "f.pgm").read_bytes()
+    assert data.startswith(b"P5\n4 3\n255\n") and len(data) == len(b"P5\n4 3\n255\n") + 12
+    img = np.frombuffer(data[-12:], dtype=np.uint8).reshape(3, 4)
+    assert img[-1, 0] == 0 and img[0, -1] == 255   # rows stored top (largest y) first
+    with pytest.raises(ValueError):
+        tomo.save_field(str(tmp_path / "f.png"), f)

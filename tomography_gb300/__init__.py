@@ -107,6 +107,7 @@ def library() -> C.CDLL:
         "tomo_poll": (I, [P, C.c_uint64, dp]),
         "tomo_cancel": (I, [P, C.c_uint64]),
         "tomo_get_stats": (I, [P, C.POINTER(Stats)]),
+        "tomo_field_snapshot": (I, [P, SZ, I, I, fp, SZ]),
         "tomo_trace_misfit_static": (I, [C.c_void_p, C.c_void_p, SZ, SZ, SZ, C.c_void_p, C.c_void_p]),
         "tomo_last_error": (C.c_char_p, []),
         "tomo_version": (C.c_char_p, []),
@@ -146,6 +147,22 @@ def breast_spec(config: int) -> Spec:
     s = Spec()
     _check(library().tomo_spec_breast(C.byref(s), int(config)))
     return s
+
+
+def save_field(path: str, field: np.ndarray) -> None:
+    """Write a field snapshot: ``.npy`` keeps the values; ``.pgm`` writes an 8-bit
+    grey image with zero at mid-grey, scaled to the largest magnitude."""
+    a = np.asarray(field, dtype=np.float32)
+    if path.endswith(".npy"):
+        np.save(path, a)
+        return
+    if not path.endswith(".pgm"):
+        raise ValueError("field snapshots are written as .npy or .pgm")
+    peak = float(np.abs(a).max()) or 1.0
+    img = np.clip(np.rint(127.5 + 127.5 * a / peak), 0, 255).astype(np.uint8)[::-1]   # y up
+    with open(path, "wb") as fp:
+        fp.write(b"P5\n%d %d\n255\n" % (img.shape[1], img.shape[0]))
+        fp.write(img.tobytes())
 
 
 def serving_spec(edge: int, n_antennas: int) -> Spec:
@@ -279,6 +296,17 @@ class Solver:
 
     def cancel(self, ticket: int) -> None:
         _check(library().tomo_cancel(self._h, C.c_uint64(ticket)))
+
+    FIELDS = {"ez": 0, "hx": 1, "hy": 2}
+
+    def field_snapshot(self, candidate: int = 0, excitation: int = 0, field: str = "ez") -> np.ndarray:
+        """Final Ez ((ny+1) x (nx+1)), Hx or Hy (ny x nx) of one solve of the last
+        batch, as float32 [y][x]."""
+        f = self.FIELDS[field.lower()]
+        nx, ny = self.spec.nx, self.spec.ny
+        out = np.zeros((ny + 1, nx + 1) if f == 0 else (ny, nx), dtype=np.float32)
+        _check(library().tomo_field_snapshot(self._h, int(candidate), int(excitation), f, _fptr(out), out.size))
+        return out
 
     def stats(self) -> dict:
         st = Stats()

@@ -111,6 +111,11 @@ int tomo_get_stats(tomo_handle* h, tomo_stats* stats) {
     return h->eng->stats(stats);
 }
 
+int tomo_field_snapshot(tomo_handle* h, size_t candidate, int excitation, int field, float* out, size_t n) {
+    if (!h) return fail(TOMO_EINVAL, "NULL handle");
+    return h->eng->snapshot(candidate, excitation, field, out, n);
+}
+
 const char* tomo_last_error(void) { return tomo::g_last_error.c_str(); }
 const char* tomo_version(void) { return "tomography_gb300 0.1"; }
 

@@ -753,6 +753,8 @@ int EngineT<Real>::forward(const double* args, size_t ncand, size_t nparam, cons
     stats_.total_ms = tot;
     stats_.cell_updates = (double)nsolves * (double)s.nx * (double)s.ny * (double)pc.S;
     stats_.launches = s.plain ? (int64_t)pc.S * nsolves : nlaunch;
+    have_batch_ = true;
+    last_parity_ = s.plain ? 0 : (nlaunch & 1);   // the plain path updates copy 0 in place
     stats_.kernels = kernels;
     stats_.steps_per_launch = blk_.T;
     stats_.cols_per_lane = blk_.cols;
@@ -760,6 +762,25 @@ int EngineT<Real>::forward(const double* args, size_t ncand, size_t nparam, cons
     stats_.h2d_bytes = h2d;
     stats_.d2h_bytes = d2h;
     if (flag && s.mode != TOMO_MODE_REFERENCE_GPU) return fail(TOMO_ENUMERIC, "non-finite field or fitness detected");
+    return TOMO_OK;
+}
+
+template <typename Real>
+int EngineT<Real>::snapshot(size_t cand, int exc, int field, float* out, size_t n) {
+    const ProblemClass& pc = cd_.pc;
+    if (!have_batch_) return fail(TOMO_ENOTREADY, "no batch has run on this handle yet");
+    if (field < TOMO_FIELD_EZ || field > TOMO_FIELD_HY) return fail(TOMO_EINVAL, "field must be 0 (Ez), 1 (Hx) or 2 (Hy)");
+    if (exc < 0 || exc >= pc.n_exc || cand >= (size_t)cur_cand_)
+        return fail(TOMO_EINVAL, "candidate or excitation out of range of the last batch");
+    const size_t rows = field == TOMO_FIELD_EZ ? pc.ny + 1 : pc.ny, cols = field == TOMO_FIELD_EZ ? pc.nx + 1 : pc.nx;
+    if (!out || n < rows * cols) return fail(TOMO_EINVAL, "snapshot needs " + std::to_string(rows * cols) + " values");
+    const SolveDesc<Real>& D = h_descs_[cand * pc.n_exc + exc];
+    const Real* src = (field == TOMO_FIELD_EZ ? D.ez : field == TOMO_FIELD_HX ? D.hx : D.hy)[last_parity_];
+    std::vector<Real> host(rows * cols);
+    CUDA_TRY(cudaMemcpy2DAsync(host.data(), cols * sizeof(Real), src, (size_t)pc.pitch * sizeof(Real),
+                               cols * sizeof(Real), rows, cudaMemcpyDeviceToHost, stream_));
+    CUDA_TRY(cudaStreamSynchronize(stream_));
+    for (size_t i = 0; i < host.size(); ++i) out[i] = (float)host[i];
     return TOMO_OK;
 }
 

@@ -19,6 +19,7 @@ class EngineBase {
     virtual int serve_step(int* n_active) = 0;
     virtual int poll(uint64_t ticket, double* fitness) = 0;
     virtual int cancel(uint64_t ticket) = 0;
+    virtual int snapshot(size_t cand, int exc, int field, float* out, size_t n) = 0;
 };
 
 int fail(int code, const std::string& msg);

@@ -486,6 +486,7 @@ class EngineT : public EngineBase {
     int serve_step(int* n_active) override;
     int poll(uint64_t ticket, double* fitness) override;
     int cancel(uint64_t ticket) override;
+    int snapshot(size_t cand, int exc, int field, float* out, size_t n) override;
 
    private:
     int ensure_batch(int ncand);
@@ -504,6 +505,8 @@ class EngineT : public EngineBase {
     cudaEvent_t ev_[4] = {nullptr, nullptr, nullptr, nullptr};
     int num_sms_ = 0;
     Blocking blk_;                                 // blocking of the next batch
+    bool have_batch_ = false;                      // a batch's final state is on the device
+    int last_parity_ = 0;                          // ping-pong copy holding that state
     bool auto_T_ = false, auto_cols_ = false, auto_minb_ = false;   // tuned per batch size on first use
     int fix_T_ = 0, fix_cols_ = 0, fix_minb_ = 0;  // dimensions fixed by the spec or the environment
     std::map<int, Blocking> tuned_;                // solves per batch -> blocking
