@@ -6,7 +6,7 @@
 // W = P - 2T of them) and recomputes the T columns on either side as halo.
 // Strips near the left and right edges (PEC boundary, CPML, vertical NTFF
 // faces) use the narrow COLS = 1 layout inside the same launch, so that the
-// general path below runs on as few lanes as possible.  The warp sweeps the
+// special handling below runs on as few lanes as possible.  The warp sweeps the
 // strip bottom-to-top, one row per iteration, and carries T time levels in
 // flight: level k receives row r-2k (from level k-1 one iteration earlier),
 // advances row r-2k-1 from time n0+k to n0+k+1 and hands it to level k+1.
@@ -15,13 +15,21 @@
 // Levels are processed in descending order so that no level waits on another
 // inside an iteration (independent instruction streams for the scheduler).
 //
-// Two code paths per (row, level), chosen warp-uniformly:
-//  * fast path: interior rows of interior strips (no CPML, no boundary, no
-//    NTFF face, no source or receiver, no plane-wave cell) -- the plain Yee +
-//    Debye update;
-//  * general path: everything else.
-// Both evaluate the same explicitly rounded formulas, so a cell gives the
-// same bits whichever path computes it.
+// Code paths, chosen warp-uniformly:
+//  * interior block: every level of the iteration on an interior row of a
+//    strip without special columns -- all T levels as one straight-line block,
+//    so the scheduler interleaves their independent dependency chains;
+//  * edge block (breast mode): the same for the narrow edge strips, with the
+//    x-CPML terms computed on every lane and chosen per lane by select;
+//  * otherwise per level: the fast path (interior rows, and in breast mode the
+//    y-CPML rows), the edge path (other rows of the narrow strips, breast
+//    mode) or the general path (boundary rows, NTFF face rows, source and
+//    receiver rows, and in the reference modes the edge strips and the
+//    plane-wave rows).
+// All evaluate the same explicitly rounded formulas, so a cell gets the same
+// bits whichever path computes it.  The running DFT of the NTFF contour is a
+// separate kernel (dft_accumulate_kernel): the sweep only stores each level's
+// contour samples.
 //
 // Physics per cell follows the reference kernels:
 //   H update  FDTD_GPU.cu:298-355  (Hy += Chez dEz/dx, Hx -= Chez dEz/dy, CPML psi)
@@ -41,8 +49,8 @@ namespace tomo {
 // One vertical strip of one solve: owned columns [x0, x1) of solve `solve`.
 // Narrow items (COLS = 1 layout, 32 - 2T owned columns) cover the CPML,
 // boundary and vertical NTFF-face columns near the left and right edges, where
-// the general path runs on every row; wide items (the kernel's COLS) cover the
-// interior, whose halo stays clear of those columns.
+// every row needs per-lane special handling; wide items (the kernel's COLS)
+// cover the interior, whose halo stays clear of those columns.
 //
 // A strip may be cut into row segments (owned rows [y0, y1)) when a batch has
 // too few strips to fill the GPU.  A segment's sweep starts 2T rows below y0
