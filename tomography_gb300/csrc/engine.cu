@@ -5,8 +5,10 @@
 //         triples and ellipse geometry (FDTD_GPU.cu:657-693 / FDTD_CPU.cxx:682-698)
 //   H2D : one packed upload
 //   GPU : material maps + FP64 coefficient tables, zero state, a CUDA graph of
-//         ceil(steps/T) advance launches (each followed by a progress bump),
-//         far field, misfit
+//         ceil(steps/T) advance launches (each followed by the running DFT of
+//         the NTFF contour and a progress bump), far field, misfit; the
+//         blocking of the advance kernel is autotuned on the first batch of
+//         each size
 //   D2H : fitness (plus optional traces / far field)
 // Device buffers persist across calls (the reference allocates and frees ~30
 // buffers inside every call, FDTD_GPU.cu:858-1106).
@@ -682,7 +684,8 @@ int EngineT<Real>::forward(const double* args, size_t ncand, size_t nparam, cons
                              stream_));
     h2d += sizeof(SolveDesc<Real>) * nsolves;
 
-    // time loop: ceil(S/T) advance launches + progress bumps, replayed as one CUDA graph
+    // time loop: ceil(S/T) advance launches, each followed by the running DFT and
+    // the progress bump, replayed as one CUDA graph
     const int nlaunch = (pc.S + blk_.T - 1) / blk_.T;
     if (s.plain) {
         // plain baseline path: one solve per launch, one launch per field update
