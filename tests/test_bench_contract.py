@@ -1,0 +1,39 @@
+"""CPU: the reference arm of bench.py keeps its output contract.
+
+One JSON line with the run's metric and unit, "impl": "reference", a
+cpu_baseline block describing the run and an e2e block without host-device
+bytes; ranks other than 0 print nothing and exit 0.
+"""
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+import sys
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _run(env_extra):
+    env = dict(os.environ, **env_extra)
+    return subprocess.run([sys.executable, os.path.join(REPO, "bench.py"), "--impl", "reference", "--steps", "1",
+                           "--warmup", "0"], capture_output=True, text=True, env=env, timeout=600, cwd=REPO)
+
+
+def test_reference_arm_json_line():
+    out = _run({})
+    assert out.returncode == 0, out.stderr
+    lines = [l for l in out.stdout.splitlines() if l.strip()]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["metric"] == "PSO fitness evals/s" and d["unit"] == "evals/s"
+    assert d["value"] > 0 and d["steps"] == 1 and d["higher_is_better"] is True
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["kind"] == "port" and cb["cores"] >= 1 and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert d["config"]["grid"] == 400 and d["config"]["steps_per_solve"] == 3000
+
+
+def test_reference_arm_other_ranks_are_silent():
+    out = _run({"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"})
+    assert out.returncode == 0 and out.stdout.strip() == ""
