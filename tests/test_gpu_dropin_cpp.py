@@ -3,8 +3,9 @@
 A small C++ program includes ``tomography_fdtd.hpp``, takes ``FDTD_GPU`` as a
 ``double (*)(const std::vector<double>&)`` -- the function-pointer type
 tao's ``ps.go(FDTD_GPU)`` receives (test.cxx:94-121) -- and links the
-library.  The target is read from TOMO_MEASUREMENT_FILE, as raw float32 and
-as text.  Two calls in a row must give exactly the fitness of the batch API
+library.  The target is read from TOMO_MEASUREMENT_FILE, as raw float32, as
+text, and as the reference's whole 8000-entry array (of which its misfit uses
+the first 4000).  Two calls in a row must give exactly the fitness of the batch API
 for the same arguments, and a short argument vector must throw
 std::out_of_range (the reference's ``.at()``).
 """
@@ -78,7 +79,9 @@ def test_cpp_dropin_matches_batch_api(tomo, tmp_path):
     meas.tofile(raw)
     txt = tmp_path / "measurement.txt"
     txt.write_text("\n".join(repr(float(v)) for v in meas))
-    for path in (raw, txt):
+    full = tmp_path / "measurement8000.f32"   # the reference's whole 8000-entry array: first 4000 used
+    np.load(os.path.join(REPO, "tests", "golden", "ref_measurement_gpu.npy")).astype(np.float32).tofile(full)
+    for path in (raw, txt, full):
         env = dict(os.environ, TOMO_MEASUREMENT_FILE=str(path))
         out = subprocess.run([str(exe)] + [repr(float(a)) for a in args], env=env, capture_output=True, text=True,
                              timeout=600)

@@ -83,6 +83,11 @@ double FDTD_GPU(const std::vector<double>& arguments) {
         const char* path = std::getenv("TOMO_MEASUREMENT_FILE");
         if (!path) throw std::runtime_error("FDTD_GPU: no target; set TOMO_MEASUREMENT_FILE or call tomo_fdtd_gpu_set_target");
         std::vector<float> t = read_target_file(path);
+        // the reference's misfit reads the first E*F*A = 4000 entries of its
+        // target array (FDTD_GPU.cu:996-1008, an 8000-entry literal): a longer
+        // file is used the same way
+        const size_t n_target = (size_t)spec.n_excitations * spec.nfreq * spec.n_angles;
+        if (t.size() > n_target) t.resize(n_target);
         int rc = tomo_set_target(h, t.data(), t.size());
         if (rc) throw_status(rc, "tomo_set_target");
         g_target_set = true;
