@@ -11,8 +11,10 @@
 // Differences by design:
 //  * the far-field target vector is data, not a compiled literal
 //    (FDTD_GPU.cu:996): it is read once from the file named by the
-//    environment variable TOMO_MEASUREMENT_FILE (4000 float32 values, raw
-//    little-endian, or whitespace-separated text), or set explicitly with
+//    environment variable TOMO_MEASUREMENT_FILE (raw little-endian float32,
+//    or numbers separated by spaces, commas or newlines; as in the
+//    reference's misfit the first 4000 values are used, so its whole
+//    8000-entry array works as is), or set explicitly with
 //    tomo_fdtd_gpu_set_target();
 //  * errors throw instead of exit(-1) (FDTD_GPU.cu:35-48): std::out_of_range
 //    for a short argument vector (the reference's .at()), std::runtime_error
