@@ -149,15 +149,30 @@ def cpu_baseline_sample(spec_dict: dict, params: np.ndarray, threads: int) -> tu
     return 1.0 / dt, {"seconds": dt, "solves": len(probs)}
 
 
+def workload_config(world: int, ncand: int) -> dict:
+    """The benchmarked workload (breast-imaging workload 1), identical in both arms."""
+    return {"workload": "breast-imaging PSO generation (batched fitness)", "grid": 400, "dx_mm": 0.5,
+            "cpml_cells": 12, "steps_per_solve": 3000, "candidates_per_gpu": ncand, "tx_per_candidate": 16,
+            "solves_per_step": ncand * 16, "params_per_candidate": 64, "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2 (%.0f GB state)" % (ncand * 16 * 400 * 400 * 4 * 8 / 1e9)}
+
+
 def run_reference(args) -> None:
+    """Reference arm: the reference's CPU algorithm for this workload, timed on
+    the host cores.  The reference's own FDTD_CPU.cxx only runs its compiled-in
+    plane-wave problem, so the arm runs the oracle's FP32 port of it in the
+    breast-imaging mode (checker-side spec and candidates; the product library
+    is not loaded), one candidate per step, one solve per host thread.  The
+    per-evaluation work (16 solves of 400 x 400 x 3000 steps) is that of one
+    candidate of the GPU arm's generation."""
     rank, world, _ = _rank_info()
     if rank != 0:
         return
-    import tomography_gb300 as T
-    from tomography_gb300 import workloads as W
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import model as M  # the oracle (reference arm)
 
-    spec = T.breast_spec(CONFIG_INDEX).as_dict()
-    cand = W.candidate_batch(CONFIG_INDEX, 1, spec["n_ellipses"])[0]
+    spec = M.breast_spec(CONFIG_INDEX)
+    cand = M.workload_candidates(CONFIG_INDEX, 1, spec["n_ellipses"])[0]
     threads = os.cpu_count() or 1
     for _ in range(args.warmup):
         cpu_baseline_sample(spec, cand, threads)
@@ -172,15 +187,54 @@ def run_reference(args) -> None:
         "impl": "reference", "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded candidates)",
-        "config": {"workload": "breast-imaging PSO generation: 400x400, 12-cell CPML, 3000 steps, 16 tx/candidate, "
-                               "8 ellipses (64 params); reference arm = 1 candidate per step",
-                   "grid": 400, "steps_per_solve": 3000, "tx_per_candidate": 16, "parallelism": "host threads"},
+        "config": workload_config(world, args.candidates),
         "cpu_baseline": {"value": value, "unit": "evals/s", "cores": threads, "kind": "port",
-                         "sample": "1 candidate (16 transmitter solves, 400x400 x 3000 steps) per step, "
-                                   "one solve per host thread, oracle FP32 port of FDTD_CPU.cxx"},
+                         "sample": "each step: 1 candidate of the generation (16 transmitter solves, 400x400 x 3000 "
+                                   "steps; the same per-evaluation work as the GPU arm), one solve per host thread, "
+                                   "oracle FP32 port of FDTD_CPU.cxx"},
         "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def run_cpu_reference(args) -> None:
+    """The reference's own CPU solver (FDTD_CPU.cxx, compiled unchanged from the
+    reference sources or their staged copy) timed on the host cores at its
+    compile-time problem (401 x 401, 2000 steps, 4 plane waves, 10 DFT
+    frequencies): one excitation of --cpu-steps steps per copy, one copy on
+    one core (latency) and one copy per core on every core (throughput, as
+    the reference farms one evaluation per MPI rank), built without and with
+    flush-to-zero (-ffast-math).  An evaluation is 4 excitations of 2000 steps."""
+    rank, _, _ = _rank_info()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import build as OB  # checker build recipes
+
+    if not (OB.build_reference() and OB.build_reference(ftz=True)):
+        print(json.dumps({"workload": "cpu-reference", "unavailable": "reference CPU sources not staged"}))
+        return
+    import tempfile
+
+    cores = os.cpu_count() or 1
+    steps = args.cpu_steps
+    res = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        apath = os.path.join(tmp, "args.txt")
+        np.savetxt(apath, [4.0] * 81 + [0.05] * 81, fmt="%.17g")   # eps_r 4, sigma 0.05 S/m in the 9x9 patches
+        for name, exe in (("no_ftz", OB.ref_driver_path()), ("ftz", OB.ref_driver_ftz_path())):
+            for label, n in (("1_core", 1), ("all_cores", cores)):
+                out = subprocess.run([exe, "bench", apath, str(steps), str(n)], capture_output=True, text=True,
+                                     check=True).stdout
+                sec = float(out.split()[1])
+                evals = n / (4 * sec * 2000.0 / steps)
+                res[f"{name}_{label}"] = {"seconds": sec, "copies": n, "evals_per_s": evals,
+                                          "s_per_eval": n / evals,
+                                          "mcell_updates_per_s": n * 401 * 401 * steps / sec / 1e6}
+    print(json.dumps({"workload": "cpu-reference", "what": "reference FDTD_CPU.cxx time loop (H, E, 10-frequency "
+                      "running DFT), 401x401, eps_r 4 / sigma 0.05 patches; eval = 4 excitations x 2000 steps",
+                      "steps_timed_per_copy": steps, "cores": cores, "machine": os.uname().machine,
+                      "results": res}), flush=True)
 
 
 def run_ours(args) -> None:
@@ -316,12 +370,8 @@ def run_ours(args) -> None:
         "warmup": args.warmup, "ms_per_step": 1e3 * tot_dev / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded candidates and target phantom)",
-        "config": {"workload": "breast-imaging PSO generation (batched fitness)", "grid": 400, "dx_mm": 0.5,
-                   "cpml_cells": 12, "steps_per_solve": spec.steps, "candidates_per_gpu": ncand,
-                   "tx_per_candidate": spec.n_tx, "solves_per_step": ncand * spec.n_tx, "params_per_candidate": 64,
-                   "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (%.0f GB state)" % (
-                       ncand * spec.n_tx * 400 * 400 * 4 * 8 / 1e9),
-                   "steps_per_launch": st["steps_per_launch"], "cols_per_lane": st["cols_per_lane"],
+        "config": workload_config(world, ncand),
+        "tuning": {"steps_per_launch": st["steps_per_launch"], "cols_per_lane": st["cols_per_lane"],
                    "autotune": tune},
         "e2e": {"value": e2e, "unit": "evals/s", "h2d_bytes_per_step": int(st["h2d_bytes"]),
                 "d2h_bytes_per_step": int(st["d2h_bytes"])},
@@ -510,7 +560,8 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--candidates", type=int, default=N_CAND)
     ap.add_argument("--no-extras", action="store_true")
-    ap.add_argument("--workload", default="pso", choices=["pso", "serving", "large"])
+    ap.add_argument("--workload", default="pso", choices=["pso", "serving", "large", "cpu-reference"])
+    ap.add_argument("--cpu-steps", type=int, default=2000, help="cpu-reference: steps timed per copy")
     ap.add_argument("--large-steps", type=int, default=0, help="large: override the 20000 steps")
     ap.add_argument("--large-candidates", type=int, default=2, help="large: candidates timed")
     ap.add_argument("--large-check-tx", type=int, default=2, help="large: transmitters compared with FP64")
@@ -522,7 +573,9 @@ def main() -> None:
                     help="serving: capacity (Gcell-updates/s, about the batch path's measured rate) that, "
                          "with --utilisation, sets the arrival rate")
     args = ap.parse_args()
-    if args.workload == "serving" and args.impl == "ours":
+    if args.workload == "cpu-reference":
+        run_cpu_reference(args)
+    elif args.workload == "serving" and args.impl == "ours":
         run_serving(args)
     elif args.workload == "large" and args.impl == "ours":
         run_large(args)

@@ -114,6 +114,11 @@ typedef struct tomo_stats {
     int32_t tuned_configs;    /* blockings the autotuner timed in the last call            */
     int32_t min_blocks_per_sm;/* register budget of the advance kernel used (2: 255 regs,
                                  3: 168, 4: 128 per thread)                               */
+    /* serving loop, as of the end of the last tomo_serve_step */
+    uint64_t serve_bytes_in_use;  /* device bytes held by admitted requests               */
+    int32_t serve_running;        /* admitted requests still advancing                    */
+    int32_t serve_queued;         /* requests waiting for memory or solve slots           */
+    int32_t serve_running_solves; /* solves of the admitted requests                      */
 } tomo_stats;
 
 /* ---- presets */
@@ -165,6 +170,10 @@ int tomo_submit_spec(tomo_handle *h, const tomo_spec *spec, const double *args, 
                      uint64_t *ticket);
 /* target of requests that carry `spec` (NULL = the handle's spec) */
 int tomo_set_target_spec(tomo_handle *h, const tomo_spec *spec, const float *target, size_t n);
+/* device bytes a request of n_cand candidates with `spec` (NULL = the handle's
+   spec) holds while admitted: what the HBM budget of tomo_set_memory_budget is
+   charged.  No counterpart in the reference. */
+int tomo_request_bytes(tomo_handle *h, const tomo_spec *spec, size_t n_cand, uint64_t *bytes);
 /* advance every admitted solve by one launch; admits queued work first          */
 int tomo_serve_step(tomo_handle *h, int *n_active);
 /* fitness of a finished ticket (n_cand values), TOMO_ENOTREADY while running    */
@@ -182,8 +191,13 @@ int tomo_cancel(tomo_handle *h, uint64_t ticket);
    fixed device array of the library: at most 65536 solves (n_cand * n_tx)
    per call, about 1 MiB that every GPU loading the library holds until exit;
    larger problems return TOMO_EINVAL.  The first call on a device looks the
-   array up, so make it before any stream capture.  All calls share the array:
-   calls whose kernels overlap on the GPU race and must not be issued. */
+   array up, so make it before any stream capture; the address is kept for
+   the life of the process, so do not call this across a cudaDeviceReset.
+   All calls share the array: calls whose kernels overlap on the GPU race and
+   must not be issued.  The call is asynchronous and reports no numeric
+   status: a non-finite trace or target value gives a NaN or infinite
+   fitness for that candidate (check the results; the batch path's
+   tomo_forward returns TOMO_ENUMERIC instead). */
 int tomo_trace_misfit_static(const float *traces, const float *target, size_t n_cand, size_t n_tx,
                              size_t n_per_solve, double *fitness, void *stream);
 

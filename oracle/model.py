@@ -322,3 +322,76 @@ def breast_forward(spec: dict, params: np.ndarray, steps: int | None = None, bit
         out["D"] = np.stack([d for d, _ in DP])
         out["P"] = np.stack([p for _, p in DP])
     return out
+
+
+# ----------------------------------------------------------------- workload presets (checker side)
+# The breast-imaging workloads restated here as plain numbers, so that the
+# CPU baseline and the reference arm of the benchmark build their problems
+# without loading the product library; tests/test_oracle.py checks them field
+# by field against the product's presets.
+def _breast_derived(s: dict) -> dict:
+    s["dt"] = 0.99 * s["dx"] / (C0 * math.sqrt(2.0))
+    s.update(cpml_grading=3.0, cpml_sigma_max=0.8 * 4 / (ETA0 * s["dx"]), cpml_kappa_max=5.0, cpml_alpha_max=0.05,
+             cpml_alpha_min=0.0, tau=13e-12, bg_eps_inf=9.0, bg_del_eps=0.0, bg_sigma=0.0, src_f0=6e9)
+    fmax = C0 / (20 * s["dx"] * math.sqrt(s["bg_eps_inf"]))
+    band = max(fmax - s["src_f0"], 1e9)
+    s["src_tau"] = math.sqrt(math.log(10.0)) / (PI * band)
+    s.update(src_t0=4 * s["src_tau"], src_amp=0.0, nf2ff_d=s["ncpml"] + 3, ff_norm=0, misfit=2)
+    return s
+
+
+def breast_spec(config: int) -> dict:
+    """Breast-imaging workload `config` (0: plain forward solve, 1: PSO
+    generation, 2: precision study, 3: serving request, 4: large batch)."""
+    s = dict(mode=2, precision=0, dx=0.5e-3, nx=200, ny=200, steps=1000, ncpml=10, n_ellipses=3, n_antennas=16,
+             n_tx=1, antenna_radius=45e-3, nfreq=3, freqs=[3e9, 6e9, 9e9], n_angles=72, disc_radius=35e-3,
+             disc_eps_inf=3.1, disc_del_eps=1.6, disc_sigma=0.036)
+    if config == 1:
+        s.update(nx=400, ny=400, ncpml=12, steps=3000, n_ellipses=8, n_tx=16)
+    elif config == 2:
+        s.update(nx=600, ny=600, dx=0.25e-3, ncpml=12, steps=6000, n_antennas=32, n_tx=32, antenna_radius=70e-3,
+                 nfreq=8, freqs=[2e9 + 1e9 * f for f in range(8)], n_angles=360)
+    elif config == 3:
+        s.update(nx=256, ny=256, dx=0.1 / 256, ncpml=10, steps=4 * 256, n_ellipses=8, n_tx=16,
+                 antenna_radius=42e-3)
+    elif config == 4:
+        s.update(nx=2048, ny=2048, dx=0.125e-3, ncpml=16, steps=20000, n_antennas=32, n_tx=32, n_ellipses=16,
+                 antenna_radius=70e-3, disc_eps_inf=15.9, disc_del_eps=23.8, disc_sigma=0.83, nfreq=16,
+                 freqs=[1e9 + 0.5e9 * f for f in range(16)], n_angles=720)
+    elif config != 0:
+        raise ValueError("breast config must be 0..4")
+    return _breast_derived(s)
+
+
+_MASK64 = (1 << 64) - 1
+
+
+def _splitmix_uniforms(seed: int):
+    """splitmix64 -> uniform doubles in [0, 1) (the workloads' seeded generator)."""
+    state = seed & _MASK64
+    while True:
+        state = (state + 0x9E3779B97F4A7C15) & _MASK64
+        z = state
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & _MASK64
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & _MASK64
+        yield ((z ^ (z >> 31)) >> 11) * (1.0 / (1 << 53))
+
+
+def candidate_params(seed: int, n_ellipses: int, disc_radius: float = 35e-3) -> np.ndarray:
+    """One PSO candidate: per ellipse a centre uniform in the disc, semi-axes in
+    [2, 15] mm, angle in [0, pi), eps_inf in [2, 20], del_eps in [1, 40],
+    sigma in [0, 1] S/m."""
+    u = _splitmix_uniforms(seed)
+    out = []
+    for _ in range(n_ellipses):
+        r = disc_radius * math.sqrt(next(u))
+        phi = 2 * math.pi * next(u)
+        out += [r * math.cos(phi), r * math.sin(phi), 2e-3 + 13e-3 * next(u), 2e-3 + 13e-3 * next(u),
+                math.pi * next(u), 2 + 18 * next(u), 1 + 39 * next(u), next(u)]
+    return np.array(out, dtype=np.float64)
+
+
+def workload_candidates(config: int, n_cand: int, n_ellipses: int, disc_radius: float = 35e-3) -> np.ndarray:
+    """Candidates 0..n_cand-1 of workload `config` (seed 0x70F00000 + config + 1000 k)."""
+    seed = 0x70F00000 + config
+    return np.stack([candidate_params(seed + 1000 * k, n_ellipses, disc_radius) for k in range(n_cand)])

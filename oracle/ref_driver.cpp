@@ -2,7 +2,7 @@
 //
 // This file is part of the oracle (checker) only: it is linked against the
 // reference sources FDTD_CPU.cxx and FDTD_common.cxx, compiled unchanged from
-// the reference tree by oracle/build_ref.py, and is used to produce the golden
+// the reference sources by oracle/build.py, and is used to produce the golden
 // vectors under tests/golden/.  Nothing in the product links or runs it.
 //
 // Modes
@@ -16,11 +16,18 @@
 //       and dumps intermediate observables: Ez probe traces, the final fields
 //       of excitation 0, the running-DFT surface currents, and the far-field
 //       magnitudes D from N2FPostProcess (FDTD_CPU.cxx:538-614).
+//   bench <args.txt> <nsteps> <nthreads>
+//       Times the reference's own time loop (FDTD_CPU.cxx:803-813: H update,
+//       E update, running DFT at every frequency) for <nsteps> steps of one
+//       plane-wave excitation, in <nthreads> independent copies run at once
+//       (one per host thread, as the reference farms one evaluation per MPI
+//       rank).  Prints "seconds <wall> threads <n> steps <nsteps>".
 //
 // The reference's compile-time constants come from its own header
 // FDTD_common.hxx (included from the reference tree).  That header defines
 // short macros such as `d`, `dt`, `dx`, `nx`, `tau`: this file therefore uses
 // no identifier with those spellings.
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -29,6 +36,8 @@
 #include <string>
 #include <unistd.h>
 #include <fcntl.h>
+#include <chrono>
+#include <thread>
 
 #include "FDTD_common.hxx"
 
@@ -217,9 +226,74 @@ static int run_steps(const char* args_path, int nsteps, const char* out_path) {
     return 0;
 }
 
+// One independent copy of the reference time loop (FDTD_CPU.cxx:746-813 set-up
+// and stepping) for nsteps steps of excitation 0; returns a checksum so the
+// work cannot be optimised away.
+static double bench_copy(const std::vector<float>& image, int nsteps) {
+    const int NXg = nx, NYg = ny;
+    const int NEz = (NXg + 1) * (NYg + 1), NH = NXg * NYg;
+    std::vector<float> Ceze(NEz), Cezhy(NEz), Cezeic(NEz), Cezeip(NEz), Ez(NEz), eps_r(NEz), sig(NEz);
+    std::vector<float> Hy(NH), Hx(NH);
+    std::vector<float> kex(16), kmx(16), aex(16), bex(16), amx(16), bmx(16), al_e(16), al_m(16), s_e(16), s_m(16);
+    std::vector<float> psi_ezy(NXg * 20 + 64), psi_ezx(NXg * 20 + 64), psi_hyx(NYg * 20 + 64), psi_hxy(NXg * 20 + 64);
+    const int ny_side = size_y_side, nx_side = size_x_side, F = numberoffrequencies;
+    std::vector<cpu_cuComplex> cjzyp(ny_side * F), cjzyn(ny_side * F), cmxyp(ny_side * F), cmxyn(ny_side * F);
+    std::vector<cpu_cuComplex> cjzxp(nx_side * F), cjzxn(nx_side * F), cmyxp(nx_side * F), cmyxn(nx_side * F);
+    eps_r_z_init(eps_r.data(), image);
+    sigma_e_z_init(sig.data(), s_e.data(), image);
+    Ceze_init(eps_r.data(), sig.data(), Ceze.data());
+    k_e_init(kex.data());
+    k_m_init(kmx.data());
+    Cezhy_init(eps_r.data(), sig.data(), Cezhy.data(), kex.data());
+    sigma_e_pml_init(s_e.data());
+    sigma_m_pml_init(s_m.data(), s_e.data());
+    alpha_e_init(al_e.data());
+    alpha_m_init(al_e.data(), al_m.data());
+    bex_init(bex.data(), s_e.data(), kex.data(), al_e.data());
+    aex_init(aex.data(), s_e.data(), kex.data(), al_e.data(), bex.data());
+    bmx_init(bmx.data(), s_m.data(), kmx.data(), al_m.data());
+    amx_init(amx.data(), s_m.data(), kmx.data(), al_m.data(), bmx.data());
+    cpu_scattered_parameter_init(eps_r.data(), sig.data(), Cezeic.data(), Cezeip.data());
+    const float Phi = 0.f;
+    for (int it = 0; it < nsteps; ++it) {
+        cpu_H_field_update(Hy.data(), Hx.data(), Ez.data(), bmx.data(), psi_hyx.data(), amx.data(), bmx.data(),
+                           amx.data(), psi_hxy.data(), kmx.data());
+        E_field_update(&it, Ez.data(), Hy.data(), Hx.data(), psi_ezx.data(), aex.data(), aex.data(), bex.data(),
+                       bex.data(), psi_ezy.data(), kex.data(), Cezhy.data(), Cezhy.data(), Ceze.data(), Cezeip.data(),
+                       Cezeic.data(), Phi);
+        for (int fi = 0; fi < F; ++fi) {
+            float freq = startfrequency + deltafreq * fi;
+            calculate_JandM(&freq, &it, Ez.data(), Hy.data(), Hx.data(), cjzxp.data() + fi * nx_side,
+                            cjzyp.data() + fi * ny_side, cjzxn.data() + fi * nx_side, cjzyn.data() + fi * ny_side,
+                            cmxyp.data() + fi * ny_side, cmyxp.data() + fi * nx_side, cmxyn.data() + fi * ny_side,
+                            cmyxn.data() + fi * nx_side);
+        }
+    }
+    double sum = 0;
+    for (float v : Ez) sum += v;
+    return sum + cjzyn[0].r;
+}
+
+static int run_bench(const char* args_path, int nsteps, int nthreads) {
+    std::vector<double> args = read_args(args_path);
+    if (args.size() < 162) { std::fprintf(stderr, "need 162 arguments\n"); return 2; }
+    std::vector<float> image(args.begin(), args.begin() + 162);
+    std::vector<double> sums(nthreads, 0.0);
+    const auto tic = std::chrono::steady_clock::now();
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nthreads; ++t) pool.emplace_back([&, t] { sums[t] = bench_copy(image, nsteps); });
+    for (auto& th : pool) th.join();
+    const auto toc = std::chrono::steady_clock::now();
+    std::printf("seconds %.6f threads %d steps %d checksum %.9g\n", std::chrono::duration<double>(toc - tic).count(),
+                nthreads, nsteps, sums[0]);
+    return 0;
+}
+
 int main(int argc, char** argv) {
     if (argc >= 4 && std::strcmp(argv[1], "fitness") == 0) return run_fitness(argv[2], argv[3]);
     if (argc >= 5 && std::strcmp(argv[1], "steps") == 0) return run_steps(argv[2], std::atoi(argv[3]), argv[4]);
-    std::fprintf(stderr, "usage: %s fitness <args> <out> | steps <args> <nsteps> <out.bin>\n", argv[0]);
+    if (argc >= 5 && std::strcmp(argv[1], "bench") == 0)
+        return run_bench(argv[2], std::atoi(argv[3]), std::max(1, std::atoi(argv[4])));
+    std::fprintf(stderr, "usage: %s fitness <args> <out> | steps <args> <nsteps> <out.bin> | bench <args> <nsteps> <threads>\n", argv[0]);
     return 2;
 }

@@ -82,8 +82,9 @@ def main() -> None:
     if not oracle_build.build_reference():
         sys.exit("reference tree not available")
     drv = oracle_build.ref_driver_path()
-    m_cpu = extract_measurement(os.path.join(oracle_build.REFERENCE_TREE, "FDTD_CPU.cxx"), 789)
-    m_gpu = extract_measurement(os.path.join(oracle_build.REFERENCE_TREE, "FDTD_GPU.cu"), 996)
+    tree = oracle_build.reference_source_dir()
+    m_cpu = extract_measurement(os.path.join(tree, "FDTD_CPU.cxx"), 789)
+    m_gpu = extract_measurement(os.path.join(tree, "FDTD_GPU.cu"), 996)
     np.save(os.path.join(HERE, "ref_measurement_cpu.npy"), m_cpu)
     np.save(os.path.join(HERE, "ref_measurement_gpu.npy"), m_gpu)
     print("measurement vectors:", m_cpu.shape, m_gpu.shape)

@@ -37,3 +37,26 @@ def test_reference_arm_json_line():
 def test_reference_arm_other_ranks_are_silent():
     out = _run({"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"})
     assert out.returncode == 0 and out.stdout.strip() == ""
+
+
+def test_reference_arm_does_not_load_the_product():
+    """The reference arm runs the checker only: the product package is never
+    imported and its native library never mapped into the process."""
+    code = ("import sys; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '0'];"
+            "sys.path.insert(0, %r); import bench; bench.main();"
+            "maps = open('/proc/self/maps').read();"
+            "print('PRODUCT', any(m.startswith('tomography_gb300') for m in sys.modules),"
+            " 'libtomography_gb300' in maps)") % REPO
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=REPO)
+    assert out.returncode == 0, out.stderr
+    tail = [l for l in out.stdout.splitlines() if l.startswith("PRODUCT")]
+    assert tail == ["PRODUCT False False"], out.stdout[-500:]
+
+
+def test_both_arms_report_the_same_config():
+    sys.path.insert(0, REPO)
+    import bench
+
+    out = _run({})
+    d = json.loads([l for l in out.stdout.splitlines() if l.strip()][0])
+    assert d["config"] == bench.workload_config(1, bench.N_CAND)

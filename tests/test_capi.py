@@ -118,3 +118,40 @@ def test_save_field_image(tomo, tmp_path):
     assert img[-1, 0] == 0 and img[0, -1] == 255   # rows stored top (largest y) first
     with pytest.raises(ValueError):
         tomo.save_field(str(tmp_path / "f.png"), f)
+
+
+def test_dropin_target_file_rules(tomo, tmp_path):
+    """TOMO_MEASUREMENT_FILE parsing of the drop-in (no GPU needed): raw float32
+    or text, 4000 values or the reference's 8000 (first 4000 used); a .npy file,
+    text with other content, or another length is refused."""
+    meas = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_measurement_gpu.npy"))
+    meas = meas.astype(np.float32)
+    assert meas.size == 8000
+    raw = tmp_path / "m.f32"
+    meas.tofile(raw)
+    np.testing.assert_array_equal(tomo.read_target_file(str(raw)), meas[:4000])
+    meas[:4000].tofile(raw)
+    np.testing.assert_array_equal(tomo.read_target_file(str(raw)), meas[:4000])
+    txt = tmp_path / "m.txt"
+    txt.write_bytes(b"\xef\xbb\xbf" + ", ".join("%.9g" % v for v in meas[:4000]).encode() + b"\n")
+    np.testing.assert_array_equal(tomo.read_target_file(str(txt)), meas[:4000])
+    bad = {
+        "npy": None,
+        "comment": b"# magnitudes\n" + b" ".join(b"%.9g" % v for v in meas[:4000]),
+        "c_literal": b"float measurement[] = {" + b",".join(b"%.9g" % v for v in meas[:4000]) + b"};",
+        "short": meas[:3999].tobytes(),
+        "odd_length": meas[:5000].tobytes(),
+        "ragged_bytes": meas[:4000].tobytes() + b"\x01",
+    }
+    for name, data in bad.items():
+        path = tmp_path / f"bad_{name}"
+        if name == "npy":
+            path = tmp_path / "m.npy"
+            np.save(path, meas[:4000])
+        else:
+            path.write_bytes(data)
+        with pytest.raises(tomo.TomoError) as ei:
+            tomo.read_target_file(str(path))
+        assert ei.value.status == -1, name
+    with pytest.raises(tomo.TomoError):
+        tomo._target_values(meas[:5000])

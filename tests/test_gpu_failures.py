@@ -1,0 +1,76 @@
+"""Failure paths, made on the host (no GPU fault, trap or hang is involved).
+
+The reference calls exit(-1) on a CUDA error (FDTD_GPU.cu:35-48), throws
+std::out_of_range on a short argument vector (.at(), FDTD_GPU.cu:657-693) and
+silently clamps NaN fields to zero (FDTD_GPU.cu:335-350, 425-430).  Here every
+failure is a status code:
+* a candidate with a non-finite parameter is rejected with TOMO_EINVAL before
+  anything is launched (batch and serving paths);
+* an unstable candidate (permittivity 0.01: ten times the Courant limit of the
+  time step) blows up, and the non-finite detector of the misfit reports
+  TOMO_ENUMERIC instead of a fitness;
+* a batch above the device-memory budget is refused with TOMO_ENOMEM_BUDGET;
+* a fitness without a target is refused with TOMO_ENOTARGET;
+and the handle stays usable after each failure: the next valid call returns
+the same fitness as on a fresh handle.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from helpers import small_breast_spec, small_params
+
+pytestmark = pytest.mark.gpu
+
+
+def _status(tomo, fn, *a):
+    try:
+        fn(*a)
+    except tomo.TomoError as e:
+        return e.status
+    return 0
+
+
+def test_failures_are_status_codes_and_the_handle_survives(tomo):
+    from tomography_gb300 import workloads as W
+
+    spec = small_breast_spec(tomo, n_ellipses=3, steps=300)
+    good = small_params(W, 3, seed_offset=7)
+    with tomo.Solver(spec) as s:
+        target = s.forward(small_params(W, 3), traces=True, far_field=False)["traces"][0]
+    with tomo.Solver(spec) as fresh:
+        fresh.set_target(target)
+        want = fresh.fitness(good)
+    with tomo.Solver(spec) as s:
+        assert _status(tomo, s.fitness, good) == -8            # TOMO_ENOTARGET
+        s.set_target(target)
+        bad = good.copy()
+        bad[5] = np.nan                                         # eps_inf of ellipse 0
+        assert _status(tomo, s.fitness, bad) == -1              # TOMO_EINVAL, nothing launched
+        assert _status(tomo, s.fitness_batch, np.stack([good, bad])) == -1
+        assert "non-finite" in tomo.library().tomo_last_error().decode()
+        unstable = good.copy()
+        unstable[5] = 0.01                                      # 10x the Courant limit of dt
+        assert _status(tomo, s.fitness, unstable) == -4         # TOMO_ENUMERIC
+        s.set_memory_budget(1)
+        assert _status(tomo, s.fitness, good) == -2             # TOMO_ENOMEM_BUDGET
+        s.set_memory_budget(0)
+        assert s.fitness(good) == want                          # the handle is still usable
+
+
+def test_poisoned_request_is_rejected_at_submit(tomo):
+    from tomography_gb300 import workloads as W
+
+    spec = small_breast_spec(tomo, n_ellipses=3, steps=120)
+    good = small_params(W, 3, seed_offset=7)
+    bad = good.copy()
+    bad[2] = np.inf                                             # semi-axis
+    with tomo.Solver(spec) as s:
+        target = s.forward(small_params(W, 3), traces=True, far_field=False)["traces"][0]
+        s.set_target(target)
+        assert _status(tomo, s.submit, np.stack([good, bad])) == -1
+        t = s.submit(good)
+        while s.poll(t, 1) is None:
+            s.serve_step()
+        assert s.poll(t, 1)[0] == s.fitness(good)

@@ -1,0 +1,105 @@
+"""Parity at the exact sizes of the headline workloads: the CUDA path through
+the C ABI against the FP64 oracle on the same seeded inputs.
+
+* Breast workload 1, the benchmark's PSO generation: 400x400 cells, 12-cell
+  CPML, 3000 steps, 8 ellipses, all 16 transmitters.  One seeded candidate of
+  the generation and the seeded target phantom (3 fibroglandular ellipses), in
+  FP32 on the GPU: receiver traces rel-L2 <= 1e-5 for each, and the fitness
+  of the candidate against the target relative error <= 1e-6 (the targets
+  stated for the FP32 path).
+* Breast workload 0, the plain forward solve: 200x200, 1000 steps, 16
+  antennas, NTFF at 3 frequencies x 72 angles.  Traces rel-L2 <= 1e-5, far
+  field D rel-L2 <= 1e-4 (D is a float output of sums over the contour),
+  fitness relative error <= 1e-6.
+* The drop-in FDTD_GPU(arguments) at the reference's own size (401x401, 2000
+  steps, 4 plane waves, 10 frequencies x 100 angles, 3x3 Debye patches) in
+  FP32, against the FP64 oracle of the same semantics: far field D rel-L2
+  <= 1e-4 and fitness relative error <= 1e-4.  The fitness, -sum (D - m)^2 / 40
+  against the reference's own target m (FDTD_GPU.cu:996, 1004-1008), is a sum
+  of squared differences, so its relative error is about twice that of D
+  times |D| / |D - m|.
+The measured errors are printed (pytest -s) for the record.
+"""
+from __future__ import annotations
+
+import json
+import os
+
+import numpy as np
+import pytest
+
+from helpers import rel_l2
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def test_pso_workload_exact_size_vs_fp64_oracle(tomo, oracle):
+    from tomography_gb300 import workloads as W
+
+    spec = tomo.breast_spec(1)
+    assert (spec.nx, spec.ny, spec.ncpml, spec.steps, spec.n_ellipses, spec.n_tx) == (400, 400, 12, 3000, 8, 16)
+    cand = W.candidate_batch(1, 1, spec.n_ellipses)[0]
+    tparams = W.target_phantom(1, 3)
+    tspec = spec.copy(n_ellipses=3)
+    ref_t = oracle.breast_forward(tspec.as_dict(), tparams, bits=64)["traces"]
+    ref_c = oracle.breast_forward(spec.as_dict(), cand, bits=64)["traces"]
+    with tomo.Solver(tspec) as s:
+        got_t = s.forward(tparams, traces=True, far_field=False)["traces"][0]
+    target = ref_t.astype(np.float32)
+    with tomo.Solver(spec) as s:
+        s.set_target(target)
+        out = s.forward(cand[None, :], traces=True, far_field=False, fitness=True)
+    err_t = rel_l2(got_t, ref_t)
+    err_c = rel_l2(out["traces"][0], ref_c)
+    want = oracle.misfit_trace(ref_c, target)
+    err_f = abs(out["fitness"][0] - want) / abs(want)
+    print(json.dumps({"workload": 1, "target_trace_rel_l2": err_t, "candidate_trace_rel_l2": err_c,
+                      "fitness_rel": err_f, "fitness": out["fitness"][0], "oracle_fitness": want}))
+    assert err_t <= 1e-5 and err_c <= 1e-5, (err_t, err_c)
+    assert err_f <= 1e-6, (out["fitness"][0], want)
+
+
+def test_plain_forward_workload_exact_size_vs_fp64_oracle(tomo, oracle):
+    from tomography_gb300 import workloads as W
+
+    spec = tomo.breast_spec(0)
+    assert (spec.nx, spec.steps, spec.n_antennas, spec.nfreq, spec.n_angles) == (200, 1000, 16, 3, 72)
+    params = W.phantom_params(W.config_seed(0), spec.n_ellipses)
+    tparams = W.target_phantom(0, spec.n_ellipses)
+    ref = oracle.breast_forward(spec.as_dict(), params, bits=64)
+    ref_t = oracle.breast_forward(spec.as_dict(), tparams, bits=64)["traces"]
+    target = ref_t.astype(np.float32)
+    with tomo.Solver(spec) as s:
+        s.set_target(target)
+        out = s.forward(params[None, :], traces=True, far_field=True, fitness=True)
+    err_tr = rel_l2(out["traces"][0], ref["traces"])
+    err_D = rel_l2(out["D"][0], ref["D"])
+    want = oracle.misfit_trace(ref["traces"], target)
+    err_f = abs(out["fitness"][0] - want) / abs(want)
+    print(json.dumps({"workload": 0, "trace_rel_l2": err_tr, "far_field_rel_l2": err_D, "fitness_rel": err_f}))
+    assert err_tr <= 1e-5, err_tr
+    assert err_D <= 1e-4, err_D
+    assert err_f <= 1e-6, (out["fitness"][0], want)
+
+
+def test_dropin_fp32_full_size_vs_fp64_oracle(tomo, oracle):
+    from tomography_gb300 import workloads as W
+
+    meas = np.load(os.path.join(GOLD, "ref_measurement_gpu.npy"))
+    args = W.reference_patch_args(0x70F00000 + 91)
+    fit = tomo.FDTD_GPU(list(args), measurement=meas)
+    spec = tomo.reference_spec(False)
+    assert spec.precision == tomo.FP32 and (spec.nx, spec.steps) == (401, 2000)
+    with tomo.Solver(spec) as s:
+        s.set_target(meas[:4000])
+        out = s.forward(args, traces=False, far_field=True, fitness=True)
+    assert out["fitness"][0] == fit   # the drop-in is this path
+    ref = oracle.reference_forward(spec.as_dict(), args)
+    err_D = rel_l2(out["D"][0], ref["D"])
+    want = oracle.misfit_abs(ref["D"].astype(np.float32), meas, 4, 10)
+    err_f = abs(fit - want) / abs(want)
+    print(json.dumps({"dropin_fp32": True, "far_field_rel_l2": err_D, "fitness_rel": err_f, "fitness": fit,
+                      "oracle_fitness": want}))
+    assert err_D <= 1e-4, err_D
+    assert err_f <= 1e-4, (fit, want)

@@ -84,19 +84,71 @@ def test_mixed_grid_sizes_in_one_launch(tomo):
         np.testing.assert_array_equal(res[t2], want_big)
 
 
-def test_budget_admission_and_cancel(tomo):
+def test_budget_admits_requests_as_memory_frees(tomo):
+    """A budget of exactly one request's bytes: of three equal requests one is
+    admitted, the other two wait in FIFO order, and each is admitted when the
+    one before it retires and returns its memory (serve.cu admit()).  All three
+    give the batch path's fitness bit for bit."""
     from tomography_gb300 import workloads as W
 
     A = _cands(W, 2, 555)
     with _solver(tomo, W) as s:
         want = s.fitness_batch(A)
-        # a budget for about one request: the second waits, then runs
-        s.set_memory_budget(1)
+        one = s.request_bytes(len(A))
+        s.set_memory_budget(one)
+        tickets = [s.submit(A) for _ in range(3)]
+        s.serve_step()
+        st = s.stats()
+        assert st["serve_running"] == 1 and st["serve_queued"] == 2, st
+        assert st["serve_running_solves"] == len(A) * s.n_exc
+        assert st["serve_bytes_in_use"] == one
+        done, order, seen_queued = {}, [], set()
+        for _ in range(100000):
+            n = s.serve_step()
+            st = s.stats()
+            assert st["serve_bytes_in_use"] <= one and st["serve_running"] <= 1, st
+            seen_queued.add(st["serve_queued"])
+            for t in tickets:
+                if t not in done:
+                    r = s.poll(t, len(A))
+                    if r is not None:
+                        done[t] = r
+                        order.append(t)
+            if len(done) == 3 and n == 0:
+                break
+        assert order == tickets                      # FIFO: admitted one after another
+        assert {1, 0} <= seen_queued                 # the queue drained as memory freed up
+        for t in tickets:
+            np.testing.assert_array_equal(done[t], want)
+        assert s.stats()["serve_bytes_in_use"] == 0
+
+
+def test_budget_rejects_a_request_above_it(tomo):
+    from tomography_gb300 import workloads as W
+
+    A = _cands(W, 2, 556)
+    with _solver(tomo, W) as s:
+        s.set_memory_budget(s.request_bytes(len(A)) - 1)
+        t = s.submit(A)
         with pytest.raises(tomo.TomoError) as ei:
-            t = s.submit(A)
             s.serve_step()
-        assert ei.value.status == -2   # TOMO_ENOMEM_BUDGET for a request above the budget
+        assert ei.value.status == -2   # TOMO_ENOMEM_BUDGET: it can never fit
+        with pytest.raises(tomo.TomoError) as ei:
+            s.poll(t, 2)
+        assert ei.value.status == -2
+        with pytest.raises(tomo.TomoError):
+            s.poll(t, 2)                # reported once, then forgotten
         s.set_memory_budget(0)
+        t = s.submit(A)
+        assert _drain(s, [t], [2])[t].shape == (2,)
+
+
+def test_cancel(tomo):
+    from tomography_gb300 import workloads as W
+
+    A = _cands(W, 2, 557)
+    with _solver(tomo, W) as s:
+        want = s.fitness_batch(A)
         t1 = s.submit(A)
         t2 = s.submit(A)
         t3 = s.submit(A)

@@ -170,3 +170,69 @@ def test_material_coefficients_match_reference_formulas(oracle):
     assert c[3] == pytest.approx(beta / dt, rel=1e-15)
     assert c[4] == pytest.approx((-2 * eps0 * einf + 2 * eps0 - sig * dt - beta) / den, rel=1e-15)
     assert c[5] == pytest.approx((2 * eps0 * einf - 2 * eps0 - sig * dt + beta) / den, rel=1e-15)
+
+
+@pytest.mark.parametrize("config", [0, 1, 2, 3, 4])
+def test_checker_breast_presets_equal_product(tomo, oracle, config):
+    """The checker's own statement of the breast-imaging workloads (used by the
+    CPU baseline and the benchmark's reference arm, which must not load the
+    product) equals the product's presets field by field."""
+    want = tomo.breast_spec(config).as_dict()
+    got = oracle.breast_spec(config)
+    for k, v in got.items():
+        if isinstance(v, list):
+            assert np.allclose(v, want[k], rtol=1e-15, atol=0), k
+        else:
+            assert want[k] == pytest.approx(v, rel=1e-15, abs=0), k
+    for k in ("mode", "nx", "ny", "steps", "ncpml", "n_ellipses", "n_antennas", "n_tx", "nfreq", "n_angles",
+              "nf2ff_d", "misfit", "ff_norm"):
+        assert k in got, k
+
+
+def test_checker_candidates_equal_product(oracle):
+    from tomography_gb300 import workloads as W
+
+    a = oracle.workload_candidates(1, 5, 8)
+    b = W.candidate_batch(1, 5, 8)
+    np.testing.assert_array_equal(a, b)
+
+
+def test_reference_field_reset_extents_fit_the_guard():
+    """The reference's Field_reset (FDTD_GPU.cu:436-503) runs on the 19 x 19
+    grid of 22 x 22 blocks of FDTD_GPU.cu:699-703 (x, y in [0, 418)) and stores
+    zeros into the four CPML psi arrays without a grid-bounds check.  The
+    element extents of those stores, restated from :441-473, against the
+    allocations of :885-888: the reference GPU driver pads every allocation by
+    oracle/build.py's GUARD_BYTES on both sides, which must cover them."""
+    import build as oracle_build
+
+    nx = ny = 401
+    ncells = 10
+    xs = np.arange(19 * 22)
+    X, Y = np.meshgrid(xs, xs, indexing="ij")
+    idx = {"Psi_ezx": [], "Psi_ezy": [], "Psi_hyx": [], "Psi_hxy": []}
+    m = (X <= ncells) & (X != 0)
+    idx["Psi_ezx"].append((X - 1 + (Y - 1) * 20)[m])
+    m = (X >= nx - ncells) & (X != nx)
+    idx["Psi_ezx"].append((X - nx + 20 + (Y - 1) * 20)[m])
+    m = (Y <= ncells) & (Y != 0)
+    idx["Psi_ezy"].append((X - 1 + (Y - 1) * nx)[m])
+    m = (Y >= ny - ncells) & (Y != ny)
+    idx["Psi_ezy"].append((X - 1 + (Y - ny + 20) * nx)[m])
+    m = X < ncells
+    idx["Psi_hyx"].append((X + Y * 20)[m])
+    m = X >= nx - ncells
+    idx["Psi_hyx"].append((X - nx + 20 + Y * 2 * ncells)[m])
+    m = Y < ncells
+    idx["Psi_hxy"].append((X + Y * nx)[m])
+    m = Y >= ny - ncells
+    idx["Psi_hxy"].append((X + (Y - ny + 20) * nx)[m])
+    alloc = {"Psi_ezy": 20 * (nx + 1), "Psi_ezx": 20 * (ny + 1), "Psi_hyx": 20 * ny, "Psi_hxy": 20 * nx}
+    overrun = 0
+    for name, parts in idx.items():
+        i = np.concatenate(parts)
+        lo, hi = int(i.min()), int(i.max())
+        assert 4 * -lo <= oracle_build.GUARD_BYTES, (name, lo)
+        assert 4 * (hi + 1 - alloc[name]) <= oracle_build.GUARD_BYTES, (name, hi, alloc[name])
+        overrun = max(overrun, 4 * (hi + 1 - alloc[name]), -4 * lo)
+    assert overrun > 0   # the reference really does store outside its arrays

@@ -46,6 +46,17 @@ def test_static_scratch_misfit_matches_forward(tomo):
         assert rc == 0, lib.tomo_last_error()
         torch.cuda.synchronize(dev)
         np.testing.assert_array_equal(d_fit.cpu().numpy(), out["fitness"])
+    # a non-finite trace value is not an error status here (the call stays
+    # asynchronous): it shows up as a non-finite fitness of that candidate only
+    bad = d_traces.clone()
+    bad[1, 0, 0, 5] = float("nan")
+    d_fit.fill_(0.0)
+    rc = lib.tomo_trace_misfit_static(C.c_void_p(bad.data_ptr()), C.c_void_p(d_target.data_ptr()), n_cand, n_tx,
+                                      n_rx * steps, C.c_void_p(d_fit.data_ptr()), C.c_void_p(stream))
+    assert rc == 0, lib.tomo_last_error()
+    torch.cuda.synchronize(dev)
+    fit = d_fit.cpu().numpy()
+    assert np.isnan(fit[1]) and fit[0] == out["fitness"][0] and fit[2] == out["fitness"][2]
     # sizes above the static limit are rejected before any launch
     rc = lib.tomo_trace_misfit_static(C.c_void_p(d_traces.data_ptr()), C.c_void_p(d_target.data_ptr()), 70000, 1,
                                       16, C.c_void_p(d_fit.data_ptr()), C.c_void_p(stream))

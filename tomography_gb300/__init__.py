@@ -67,6 +67,10 @@ class Stats(C.Structure):
         ("tune_ms", C.c_double),
         ("tuned_configs", C.c_int32),
         ("min_blocks_per_sm", C.c_int32),
+        ("serve_bytes_in_use", C.c_uint64),
+        ("serve_running", C.c_int32),
+        ("serve_queued", C.c_int32),
+        ("serve_running_solves", C.c_int32),
     ]
 
     def as_dict(self) -> dict:
@@ -105,6 +109,7 @@ def library() -> C.CDLL:
         "tomo_set_target_spec": (I, [P, C.POINTER(Spec), fp, SZ]),
         "tomo_serve_step": (I, [P, C.POINTER(C.c_int)]),
         "tomo_poll": (I, [P, C.c_uint64, dp]),
+        "tomo_request_bytes": (I, [P, C.c_void_p, SZ, C.POINTER(C.c_uint64)]),
         "tomo_cancel": (I, [P, C.c_uint64]),
         "tomo_get_stats": (I, [P, C.POINTER(Stats)]),
         "tomo_field_snapshot": (I, [P, SZ, I, I, fp, SZ]),
@@ -113,6 +118,7 @@ def library() -> C.CDLL:
         "tomo_version": (C.c_char_p, []),
         "tomo_fdtd_gpu_set_target": (I, [fp, SZ]),
         "tomo_fdtd_gpu_release": (None, []),
+        "tomo_internal_read_target_file": (I, [C.c_char_p, fp, SZ]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -281,6 +287,14 @@ class Solver:
         t = np.ascontiguousarray(target, dtype=np.float32).ravel()
         _check(library().tomo_set_target_spec(self._h, C.byref(spec), _fptr(t), t.size))
 
+    def request_bytes(self, n_cand: int, spec: Optional[Spec] = None) -> int:
+        """Device bytes a request of n_cand candidates holds while admitted (what
+        the memory budget is charged)."""
+        b = C.c_uint64()
+        sp = C.cast(C.byref(spec), C.c_void_p) if spec is not None else None
+        _check(library().tomo_request_bytes(self._h, sp, int(n_cand), C.byref(b)))
+        return int(b.value)
+
     def serve_step(self) -> int:
         n = C.c_int()
         _check(library().tomo_serve_step(self._h, C.byref(n)))
@@ -315,6 +329,26 @@ class Solver:
 
 
 _dropin: Optional[Solver] = None
+REFERENCE_TARGET_SIZE = 4000   # E * F * A of the reference preset (4 x 10 x 100)
+
+
+def read_target_file(path: str) -> np.ndarray:
+    """The far-field target of the drop-in from a measurement file, with the
+    native library's rules: raw float32 or text (numbers separated by spaces,
+    commas or newlines), 4000 values or 8000 (magnitudes then phases) of which
+    the first 4000 are used; a .npy file or any other content raises."""
+    out = np.zeros(REFERENCE_TARGET_SIZE, dtype=np.float32)
+    n = library().tomo_internal_read_target_file(path.encode(), _fptr(out), out.size)
+    _check(n if n < 0 else TOMO_OK)
+    return out[:n]
+
+
+def _target_values(measurement) -> np.ndarray:
+    m = np.ascontiguousarray(measurement, dtype=np.float32).ravel()
+    if m.size not in (REFERENCE_TARGET_SIZE, 2 * REFERENCE_TARGET_SIZE):
+        raise TomoError(-1, f"the target needs {REFERENCE_TARGET_SIZE} values (or {2 * REFERENCE_TARGET_SIZE}: "
+                            f"magnitudes then phases), got {m.size}")
+    return m[:REFERENCE_TARGET_SIZE]
 
 
 def FDTD_GPU(arguments: Sequence[float], measurement: Optional[np.ndarray] = None) -> float:
@@ -323,7 +357,8 @@ def FDTD_GPU(arguments: Sequence[float], measurement: Optional[np.ndarray] = Non
     ``arguments``: 27 values, eps_inf of the 3x3 patches, then del_eps, then
     sigma (FDTD_GPU.cu:657-693).  Raises IndexError for a short vector (the
     reference's ``.at()`` throws std::out_of_range).  The far-field target is
-    ``measurement`` (first call) or the file named by TOMO_MEASUREMENT_FILE.
+    ``measurement`` (4000 magnitudes, or the reference's whole 8000-entry
+    array) or the file named by TOMO_MEASUREMENT_FILE (see read_target_file).
     """
     global _dropin
     args = [float(v) for v in arguments]
@@ -335,9 +370,9 @@ def FDTD_GPU(arguments: Sequence[float], measurement: Optional[np.ndarray] = Non
             path = os.environ.get("TOMO_MEASUREMENT_FILE")
             if not path:
                 raise TomoError(-8, "no target: pass measurement= or set TOMO_MEASUREMENT_FILE")
-            measurement = np.fromfile(path, dtype=np.float32)
-        solver.set_target(np.asarray(measurement, dtype=np.float32)[:4000])
+            measurement = read_target_file(path)
+        solver.set_target(_target_values(measurement))
         _dropin = solver
     elif measurement is not None:
-        _dropin.set_target(np.asarray(measurement, dtype=np.float32)[:4000])
+        _dropin.set_target(_target_values(measurement))
     return _dropin.fitness(args[:27])

@@ -96,6 +96,11 @@ int tomo_serve_step(tomo_handle* h, int* n_active) {
     return h->eng->serve_step(n_active);
 }
 
+int tomo_request_bytes(tomo_handle* h, const tomo_spec* spec, size_t n_cand, uint64_t* bytes) {
+    if (!h || !bytes) return fail(TOMO_EINVAL, "tomo_request_bytes: NULL argument");
+    return h->eng->request_bytes(spec, n_cand, bytes);
+}
+
 int tomo_poll(tomo_handle* h, uint64_t ticket, double* fitness) {
     if (!h) return fail(TOMO_EINVAL, "NULL handle");
     return h->eng->poll(ticket, fitness);

@@ -17,6 +17,7 @@ class EngineBase {
     virtual int submit_spec(const tomo_spec* spec, const double* args, size_t ncand, size_t nparam, uint64_t* ticket) = 0;
     virtual int set_target_spec(const tomo_spec* spec, const float* t, size_t n) = 0;
     virtual int serve_step(int* n_active) = 0;
+    virtual int request_bytes(const tomo_spec* spec, size_t ncand, uint64_t* bytes) = 0;
     virtual int poll(uint64_t ticket, double* fitness) = 0;
     virtual int cancel(uint64_t ticket) = 0;
     virtual int snapshot(size_t cand, int exc, int field, float* out, size_t n) = 0;

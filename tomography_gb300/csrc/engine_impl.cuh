@@ -484,6 +484,7 @@ class EngineT : public EngineBase {
     int submit_spec(const tomo_spec* spec, const double* args, size_t ncand, size_t nparam, uint64_t* ticket) override;
     int set_target_spec(const tomo_spec* spec, const float* t, size_t n) override;
     int serve_step(int* n_active) override;
+    int request_bytes(const tomo_spec* spec, size_t ncand, uint64_t* bytes) override;
     int poll(uint64_t ticket, double* fitness) override;
     int cancel(uint64_t ticket) override;
     int snapshot(size_t cand, int exc, int field, float* out, size_t n) override;

@@ -11,6 +11,7 @@
 
 #include "../../include/tomography.h"
 #include "../../include/tomography_fdtd.hpp"
+#include "engine.h"
 
 namespace {
 
@@ -22,10 +23,17 @@ void throw_status(int rc, const char* what) {
     throw std::runtime_error(std::string(what) + " failed (" + std::to_string(rc) + "): " + tomo_last_error());
 }
 
-std::vector<float> read_target_file(const char* path) {
-    std::vector<float> v;
+// Target values of a measurement file: raw little-endian float32, or text
+// (numbers separated by spaces, commas or newlines; an optional UTF-8 byte
+// order mark).  A NumPy .npy file, or text with anything else in it, is
+// rejected rather than read as numbers it does not hold.
+int read_target_file(const char* path, std::vector<float>& v, std::string& why) {
+    v.clear();
     FILE* fp = std::fopen(path, "rb");
-    if (!fp) throw std::runtime_error(std::string("cannot open TOMO_MEASUREMENT_FILE ") + path);
+    if (!fp) {
+        why = std::string("cannot open ") + path;
+        return TOMO_EINVAL;
+    }
     std::fseek(fp, 0, SEEK_END);
     long len = std::ftell(fp);
     std::fseek(fp, 0, SEEK_SET);
@@ -33,31 +41,72 @@ std::vector<float> read_target_file(const char* path) {
     size_t got = std::fread(raw.data(), 1, raw.size(), fp);
     std::fclose(fp);
     raw.resize(got);
+    static const unsigned char kNpy[6] = {0x93, 'N', 'U', 'M', 'P', 'Y'};
+    if (raw.size() >= 6 && std::memcmp(raw.data(), kNpy, 6) == 0) {
+        why = std::string(path) + " is a NumPy .npy file; write the values as raw float32 or text";
+        return TOMO_EINVAL;
+    }
+    size_t start = 0;
+    if (raw.size() >= 3 && raw[0] == 0xEF && raw[1] == 0xBB && raw[2] == 0xBF) start = 3;   // UTF-8 BOM
     // text when every byte can be part of written numbers (raw float32 data
     // almost surely holds other bytes), else raw little-endian float32
     static const char kTextBytes[] = "0123456789+-.eEinfaINFA \t\r\n,";
-    bool text = !raw.empty();
-    for (unsigned char c : raw)
-        if (c == 0 || !std::strchr(kTextBytes, c)) {
+    bool text = raw.size() > start;
+    for (size_t i = start; i < raw.size(); ++i)
+        if (raw[i] == 0 || !std::strchr(kTextBytes, raw[i])) {
             text = false;
             break;
         }
-    if (!text && raw.size() % 4 == 0) {
+    if (!text && start == 0) {
+        if (raw.size() % 4 != 0) {
+            why = std::string(path) + " is neither text nor whole float32 values";
+            return TOMO_EINVAL;
+        }
         v.resize(raw.size() / 4);
         std::memcpy(v.data(), raw.data(), raw.size());
-        return v;
+        return TOMO_OK;
     }
-    std::string s(raw.begin(), raw.end());
+    if (!text) {
+        why = std::string(path) + " holds characters that are not numbers, spaces, commas or newlines";
+        return TOMO_EINVAL;
+    }
+    std::string s(raw.begin() + start, raw.end());
     for (char& c : s) if (c == ',') c = ' ';
     const char* p = s.c_str();
-    char* end = nullptr;
     for (;;) {
+        while (*p == ' ' || *p == '\t' || *p == '\r' || *p == '\n') ++p;
+        if (!*p) break;
+        char* end = nullptr;
         float f = std::strtof(p, &end);
-        if (end == p) break;
+        if (end == p) {
+            why = std::string(path) + ": not a number at byte " + std::to_string(start + (size_t)(p - s.c_str()));
+            v.clear();
+            return TOMO_EINVAL;
+        }
         v.push_back(f);
         p = end;
     }
-    return v;
+    return TOMO_OK;
+}
+
+// The reference's misfit reads the first E*F*A = 4000 entries of its target
+// array (FDTD_GPU.cu:1004-1008), which holds 8000: the magnitudes, then the
+// phases (FDTD_GPU.cu:996).  Both lengths are accepted, and only the first
+// E*F*A values are used; any other length is an error.
+int target_values(const float* t, size_t n, size_t n_target, std::vector<float>& out, std::string& why) {
+    if (!t || (n != n_target && n != 2 * n_target)) {
+        why = "the target needs " + std::to_string(n_target) + " values (or " + std::to_string(2 * n_target) +
+              ": magnitudes then phases), got " + std::to_string(n);
+        return TOMO_EINVAL;
+    }
+    out.assign(t, t + n_target);
+    return TOMO_OK;
+}
+
+size_t reference_target_size() {
+    tomo_spec spec;
+    tomo_spec_reference(&spec, 0);
+    return (size_t)spec.n_excitations * spec.nfreq * spec.n_angles;
 }
 
 tomo_handle* handle_locked() {
@@ -82,12 +131,11 @@ double FDTD_GPU(const std::vector<double>& arguments) {
     if (!g_target_set) {
         const char* path = std::getenv("TOMO_MEASUREMENT_FILE");
         if (!path) throw std::runtime_error("FDTD_GPU: no target; set TOMO_MEASUREMENT_FILE or call tomo_fdtd_gpu_set_target");
-        std::vector<float> t = read_target_file(path);
-        // the reference's misfit reads the first E*F*A = 4000 entries of its
-        // target array (FDTD_GPU.cu:996-1008, an 8000-entry literal): a longer
-        // file is used the same way
-        const size_t n_target = (size_t)spec.n_excitations * spec.nfreq * spec.n_angles;
-        if (t.size() > n_target) t.resize(n_target);
+        std::vector<float> raw, t;
+        std::string why;
+        if (read_target_file(path, raw, why) ||
+            target_values(raw.data(), raw.size(), reference_target_size(), t, why))
+            throw std::runtime_error("FDTD_GPU: TOMO_MEASUREMENT_FILE: " + why);
         int rc = tomo_set_target(h, t.data(), t.size());
         if (rc) throw_status(rc, "tomo_set_target");
         g_target_set = true;
@@ -100,14 +148,32 @@ double FDTD_GPU(const std::vector<double>& arguments) {
 
 extern "C" int tomo_fdtd_gpu_set_target(const float* target, size_t n) {
     std::lock_guard<std::mutex> lock(g_mu);
+    std::vector<float> t;
+    std::string why;
+    if (target_values(target, n, reference_target_size(), t, why)) return tomo::fail(TOMO_EINVAL, why);
     try {
         tomo_handle* h = handle_locked();
-        int rc = tomo_set_target(h, target, n);
+        int rc = tomo_set_target(h, t.data(), t.size());
         if (rc == TOMO_OK) g_target_set = true;
         return rc;
     } catch (const std::exception&) {
         return TOMO_ECUDA;
     }
+}
+
+// Internal test hook (not part of the public ABI): the target the drop-in
+// would take from the measurement file `path` (the same parsing and length
+// rules as TOMO_MEASUREMENT_FILE), copied into out[0..cap).  Returns the
+// number of values, or a negative status with the reason in tomo_last_error().
+extern "C" int tomo_internal_read_target_file(const char* path, float* out, size_t cap) {
+    std::vector<float> raw, t;
+    std::string why;
+    if (!path) return tomo::fail(TOMO_EINVAL, "NULL path");
+    if (read_target_file(path, raw, why) || target_values(raw.data(), raw.size(), reference_target_size(), t, why))
+        return tomo::fail(TOMO_EINVAL, why);
+    if (!out || cap < t.size()) return tomo::fail(TOMO_EINVAL, "output buffer too small");
+    std::copy(t.begin(), t.end(), out);
+    return (int)t.size();
 }
 
 extern "C" void tomo_fdtd_gpu_release(void) {

@@ -13,11 +13,16 @@
 // holds it (kMaxSolves * 2 doubles + one flag, about 1 MiB) until the process
 // exits.  Host code cannot use the array's name as a device address, so the
 // first call on each device (with that device current) looks its address up
-// with cudaGetSymbolAddress and caches it; make that first call before any
-// stream capture.  All calls share the one array: the non-finite flag is
-// cleared at the start of every call and the partials are fully overwritten,
-// but two calls whose kernels overlap on the GPU (different streams, no
-// ordering between them) race on the array and must not be issued.
+// with cudaGetSymbolAddress and caches it for the life of the process; make
+// that first call before any stream capture, and do not use the entry point
+// across a cudaDeviceReset (the module may be loaded again at another
+// address).  All calls share the one array: the partials are fully
+// overwritten by every call, but two calls whose kernels overlap on the GPU
+// (different streams, no ordering between them) race on the array and must
+// not be issued.  The call stays asynchronous, so it reports no numeric
+// status: the reduction kernel raises its non-finite flag (cleared at the
+// start of every call) but nothing waits for it, and a non-finite trace
+// shows up as a NaN or infinite fitness of its candidate.
 #include <cuda_runtime.h>
 
 #include <mutex>

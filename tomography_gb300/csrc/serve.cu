@@ -180,23 +180,55 @@ int EngineT<Real>::set_target_spec(const tomo_spec* spec, const float* t, size_t
     return cd->set_target(t, n);
 }
 
+// Device memory of one request: state of every solve, material maps and
+// tables, the argument upload, far field, misfit partials and fitness, in one
+// stream-ordered allocation.
+struct RequestLayout {
+    size_t state, mats, tabs, up, ff, part, fit, total;
+};
+
+template <typename Real>
+static RequestLayout request_layout(const ClassData<Real>& cd, size_t ncand, size_t upload_doubles) {
+    const ProblemClass& pc = cd.pc;
+    const SolveLayout& L = cd.lay;
+    const size_t nsolves = ncand * (size_t)pc.n_exc;
+    auto align = [](size_t v) { return (v + 255) / 256 * 256; };
+    RequestLayout b{};
+    b.state = align(sizeof(Real) * nsolves * L.per_solve);
+    b.mats = pc.spec.mode == TOMO_MODE_BREAST ? align(L.mat_stride * ncand) : 0;
+    b.tabs = align(sizeof(Real) * kMaxMat * kMatCoef * ncand);
+    b.up = align(sizeof(double) * upload_doubles);
+    b.ff = pc.nang > 0 ? align(sizeof(float) * nsolves * pc.nfreq * pc.nang) : 0;
+    b.part = align(sizeof(double) * 2 * nsolves);
+    b.fit = align(sizeof(double) * ncand);
+    b.total = b.state + b.mats + b.tabs + b.up + 2 * b.ff + b.part + b.fit + 256;
+    return b;
+}
+
+// doubles of the packed argument upload of ncand candidates (unpack_args)
+inline size_t upload_doubles(const ProblemClass& pc, size_t ncand) {
+    const int K = pc.spec.mode == TOMO_MODE_BREAST ? pc.spec.n_ellipses : 0;
+    return ncand * kMaxMat * 3 + ncand * (size_t)K * 6;
+}
+
+template <typename Real>
+int EngineT<Real>::request_bytes(const tomo_spec* spec, size_t ncand, uint64_t* bytes) {
+    if (ncand == 0) return fail(TOMO_EINVAL, "no candidates");
+    int rc;
+    ClassData<Real>* cd = class_for(spec, &rc);
+    if (!cd) return rc;
+    *bytes = request_layout(*cd, ncand, upload_doubles(cd->pc, ncand)).total;
+    return TOMO_OK;
+}
+
 template <typename Real>
 static int admit(EngineT<Real>* eng, ServeStateT<Real>* st, ServeRequest<Real>& r, cudaStream_t stream,
                  uint64_t budget, bool* admitted) {
     *admitted = false;
     const ClassData<Real>& cd = *r.cd;
-    const ProblemClass& pc = cd.pc;
-    const SolveLayout& L = cd.lay;
-    const int ncand = (int)r.ncand;
-    auto align = [](size_t v) { return (v + 255) / 256 * 256; };
-    const size_t b_state = align(sizeof(Real) * (size_t)r.nsolves * L.per_solve);
-    const size_t b_mats = pc.spec.mode == TOMO_MODE_BREAST ? align(L.mat_stride * ncand) : 0;
-    const size_t b_tabs = align(sizeof(Real) * kMaxMat * kMatCoef * ncand);
-    const size_t b_up = align(sizeof(double) * r.up.upload.size());
-    const size_t b_ff = pc.nang > 0 ? align(sizeof(float) * (size_t)r.nsolves * pc.nfreq * pc.nang) : 0;
-    const size_t b_part = align(sizeof(double) * 2 * r.nsolves);
-    const size_t b_fit = align(sizeof(double) * ncand);
-    const size_t bytes = b_state + b_mats + b_tabs + b_up + 2 * b_ff + b_part + b_fit + 256;
+    const RequestLayout lay = request_layout(cd, r.ncand, r.up.upload.size());
+    const size_t b_state = lay.state, b_mats = lay.mats, b_tabs = lay.tabs, b_up = lay.up, b_ff = lay.ff,
+                 b_part = lay.part, b_fit = lay.fit, bytes = lay.total;
     if (st->bytes_in_use + bytes > budget) {
         if (st->bytes_in_use == 0)
             return fail(TOMO_ENOMEM_BUDGET, "request needs " + std::to_string(bytes >> 20) + " MiB, above the budget");
@@ -223,13 +255,25 @@ static int admit(EngineT<Real>* eng, ServeStateT<Real>* st, ServeRequest<Real>& 
     r.partials = (double*)p; p += b_part;
     r.fit = (double*)p; p += b_fit;
     r.flag = (int*)p;
-    int64_t kernels = 0, h2d = 0;
-    TOMO_TRY(setup_materials<Real>(cd, r.up, r.upload, r.mats, r.tabs, stream, &kernels, &h2d));
-    CUDA_TRY(cudaMemsetAsync(r.state_base, 0, b_state, stream));
-    CUDA_TRY(cudaMemsetAsync(r.flag, 0, sizeof(int), stream));
-    fill_descs<Real>(cd, r.up, r.state_base, r.mats, r.tabs, &st->hdescs[first]);
-    CUDA_TRY(cudaMemcpyAsync(st->descs.template as<SolveDesc<Real>>() + first, &st->hdescs[first],
-                             sizeof(SolveDesc<Real>) * r.nsolves, cudaMemcpyHostToDevice, stream));
+    // set-up of the admitted request; on any failure the allocation is
+    // returned at once (it was never charged to the budget)
+    auto setup = [&]() -> int {
+        int64_t kernels = 0, h2d = 0;
+        TOMO_TRY(setup_materials<Real>(cd, r.up, r.upload, r.mats, r.tabs, stream, &kernels, &h2d));
+        CUDA_TRY(cudaMemsetAsync(r.state_base, 0, b_state, stream));
+        CUDA_TRY(cudaMemsetAsync(r.flag, 0, sizeof(int), stream));
+        fill_descs<Real>(cd, r.up, r.state_base, r.mats, r.tabs, &st->hdescs[first]);
+        CUDA_TRY(cudaMemcpyAsync(st->descs.template as<SolveDesc<Real>>() + first, &st->hdescs[first],
+                                 sizeof(SolveDesc<Real>) * r.nsolves, cudaMemcpyHostToDevice, stream));
+        return TOMO_OK;
+    };
+    if (const int rc = setup()) {
+        for (int i = 0; i < r.nsolves; ++i) st->hdescs[first + i] = SolveDesc<Real>{};
+        cudaFreeAsync(r.mem, stream);
+        r.mem = nullptr;
+        r.bytes = 0;
+        return rc;
+    }
     for (int i = 0; i < r.nsolves; ++i) st->used[first + i] = 1;
     st->hi_slot = std::max(st->hi_slot, first + r.nsolves);
     st->bytes_in_use += bytes;
@@ -363,7 +407,16 @@ int EngineT<Real>::serve_step(int* n_active) {
             r.up = Unpacked{};
         }
     }
-    if (n_active) *n_active = running + (int)st->queue.size();
+    int queued = 0, solves = 0;
+    for (auto& kv : st->reqs) {
+        if (kv.second->state == kQueued) ++queued;
+        if (kv.second->state == kRunning) solves += kv.second->nsolves;
+    }
+    stats_.serve_bytes_in_use = st->bytes_in_use;
+    stats_.serve_running = running;
+    stats_.serve_queued = queued;
+    stats_.serve_running_solves = solves;
+    if (n_active) *n_active = running + queued;
     return TOMO_OK;
 }
 
@@ -374,7 +427,11 @@ int EngineT<Real>::poll(uint64_t ticket, double* fitness) {
     if (it == serve_->reqs.end()) return fail(TOMO_EINVAL, "unknown ticket");
     ServeRequest<Real>& r = *it->second;
     if (r.state == kCancelled) return fail(TOMO_ECANCELLED, "ticket was cancelled");
-    if (r.state == kFailed) return fail(r.status, "request failed");
+    if (r.state == kFailed) {
+        const int status = r.status;
+        serve_->reqs.erase(it);   // reported once, then forgotten like a finished request
+        return fail(status, "request failed");
+    }
     if (r.state != kDone) return TOMO_ENOTREADY;
     if (fitness) std::copy(r.fitness.begin(), r.fitness.end(), fitness);
     const int status = r.status;
