@@ -71,6 +71,8 @@ def test_poisoned_request_is_rejected_at_submit(tomo):
         s.set_target(target)
         assert _status(tomo, s.submit, np.stack([good, bad])) == -1
         t = s.submit(good)
-        while s.poll(t, 1) is None:
+        got = None
+        while got is None:
             s.serve_step()
-        assert s.poll(t, 1)[0] == s.fitness(good)
+            got = s.poll(t, 1)
+        assert got[0] == s.fitness(good)

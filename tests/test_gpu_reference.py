@@ -88,3 +88,32 @@ def test_dropin_fdtd_gpu(tomo):
     vac = [1.0] * 9 + [0.0] * 18
     want = -float(np.sum(meas[:4000].astype(np.float64) ** 2)) / 40.0
     assert abs(tomo.FDTD_GPU(vac) - want) <= 1e-12 * abs(want)
+
+
+@pytest.mark.parametrize("case", ["hinted", "random", "vacuum"])
+def test_dropin_vs_reference_gpu_solver(tomo, case):
+    """The drop-in FDTD_GPU(arguments) (FP32, full size) against the reference's
+    own FDTD_GPU.cu run unchanged on a GB300 (tests/golden/ref_gpu_*.npz):
+    far field D rel-L2 <= 1e-5; fitness against the reference's compiled-in
+    target relative error <= 1e-5; for the hinted phantom, whose output is
+    that target, |fitness| < 1e-9 as in the reference (-2.2e-11)."""
+    path = os.path.join(GOLD, f"ref_gpu_{case}.npz")
+    if not os.path.exists(path):
+        pytest.skip("golden fixture missing")
+    g = np.load(path)
+    meas = np.load(os.path.join(GOLD, "ref_measurement_gpu.npy"))
+    with tomo.Solver(tomo.reference_spec(False)) as s:
+        s.set_target(meas[:4000])
+        out = s.forward(g["args"], traces=False, far_field=True, fitness=True)
+    fit = tomo.FDTD_GPU(list(g["args"]), measurement=meas)
+    assert fit == out["fitness"][0]
+    D, Dref = out["D"][0].astype(np.float64), g["D"].astype(np.float64)
+    want = float(g["fitness"])
+    if case == "vacuum":
+        assert np.all(D == 0.0) and fit == pytest.approx(want, rel=1e-6)
+    elif case == "hinted":
+        assert rel_l2(D, Dref) <= 1e-5
+        assert abs(fit) < 1e-9, fit
+    else:
+        assert rel_l2(D, Dref) <= 1e-5
+        assert abs(fit - want) <= 1e-5 * abs(want), (fit, want)

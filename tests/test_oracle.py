@@ -236,3 +236,60 @@ def test_reference_field_reset_extents_fit_the_guard():
         assert 4 * (hi + 1 - alloc[name]) <= oracle_build.GUARD_BYTES, (name, hi, alloc[name])
         overrun = max(overrun, 4 * (hi + 1 - alloc[name]), -4 * lo)
     assert overrun > 0   # the reference really does store outside its arrays
+
+
+def reference_gpu_spec() -> dict:
+    """FDTD_common.hxx:3-59 with the FDTD_GPU.cu semantics (3x3 Debye patches,
+    centred plane wave, NaN clamp, absolute misfit), as plain numbers."""
+    return dict(reference_cpu_spec(), mode=0, npatch=3, pw_centred=1, nan_clamp=1, misfit=0)
+
+
+def _golden_gpu(name):
+    path = os.path.join(GOLD, f"ref_gpu_{name}.npz")
+    if not os.path.exists(path):
+        pytest.skip("golden fixture missing")
+    return np.load(path)
+
+
+@pytest.mark.parametrize("case", ["hinted", "random", "vacuum"])
+def test_oracle_fp64_vs_reference_gpu(oracle, case):
+    """The FP64 oracle in the FDTD_GPU.cu semantics against the reference's own
+    GPU solver, run unchanged on a GB300 at its full size (401x401, 2000
+    steps, 4 plane waves, Debye patches; tests/golden/make_golden_gpu.py).
+    The reference computes in float with sincosf phasors, so: running-DFT
+    surface currents rel-L2 <= 1e-5 per excitation and frequency, far field D
+    rel-L2 <= 1e-5, fitness relative error <= 1e-5 (measured: 2.6e-6, 9e-7,
+    1.2e-6).  The hinted phantom is the one whose output the reference
+    compiled in as its target (FDTD_GPU.cu:659-692, 996): its fitness is zero
+    up to float rounding, in the reference and in the oracle."""
+    g = _golden_gpu(case)
+    spec = reference_gpu_spec()
+    meas = np.load(os.path.join(GOLD, "ref_measurement_gpu.npy"))
+    out = oracle.reference_forward(spec, g["args"])
+    D, Dref = out["D"], g["D"].astype(np.float64)
+    fit = oracle.misfit_abs(D.astype(np.float32), meas, 4, 10)
+    want = float(g["fitness"])
+    if case == "vacuum":
+        assert np.all(D == 0.0) and np.all(Dref == 0.0)
+        assert fit == pytest.approx(want, rel=1e-6)
+        return
+    assert rel_l2(D, Dref) <= 1e-5
+    nx, d = 401, 100
+    l1 = nx - 2 * d - 2
+    l2, l3 = l1 + (nx - 2 * d), 2 * l1 + (nx - 2 * d)
+    for e in range(4):
+        acc = out["problems"][e].acc
+        for f in range(10):
+            J = acc[f][:, 0] + 1j * acc[f][:, 1]
+            M = acc[f][:, 2] + 1j * acc[f][:, 3]
+            ref = {k: g[k][e][f][:, 0] + 1j * g[k][e][f][:, 1]
+                   for k in ("cjzyn", "cjzxp", "cjzyp", "cjzxn", "cmxyn", "cmyxp", "cmxyp", "cmyxn")}
+            refJ = np.concatenate([ref["cjzyn"], ref["cjzxp"], ref["cjzyp"], ref["cjzxn"]])
+            refM = np.concatenate([ref["cmxyn"], ref["cmyxp"], ref["cmxyp"], ref["cmyxn"]])
+            assert len(refJ) == l3 + (nx - 2 * d) == J.size
+            assert rel_l2(J, refJ) <= 1e-5, (e, f)
+            assert rel_l2(M, refM) <= 1e-5, (e, f)
+    if case == "hinted":
+        assert abs(want) < 1e-9 and abs(fit) < 1e-9, (fit, want)
+    else:
+        assert abs(fit - want) <= 1e-5 * abs(want), (fit, want)
