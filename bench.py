@@ -360,6 +360,11 @@ def run_ours(args) -> None:
         # reported CPU baseline: oracle FP32 port of the reference CPU solver
         threads = os.cpu_count() or 1
         cb, info = cpu_baseline_sample(spec.as_dict(), cands[0], threads)
+        # a bounded sample of the serving workload (continuous batching of
+        # requests of mixed grids at Poisson arrivals), so that per-request and
+        # per-evaluation latency are part of every default run
+        if args.serving_requests > 0:
+            extra["serving_sample"] = serving_sample(args.serving_requests, 2, 8, 0.8, args.rate_gcells)
         extra["cpu_baseline"] = {"value": cb, "unit": "evals/s", "cores": threads, "kind": "port",
                                  "sample": "1 candidate = 16 transmitter solves (400x400 x 3000 steps), one per "
                                            "host thread, oracle FP32 port of FDTD_CPU.cxx (%.1f s)" % info["seconds"]}
@@ -456,34 +461,29 @@ SERVING_EDGES = (128, 256, 512, 1024)
 SERVING_ANTENNAS = (8, 16, 24, 32)
 
 
-def run_serving(args) -> None:
+def serving_sample(nreq: int, bmin: int, bmax: int, utilisation: float, rate_gcells: float) -> dict:
     """Serving workload: a differential-evolution-like client emits candidate
     batches at Poisson arrivals; each request has its own grid edge (128..1024,
     breast at 70% of the domain, 4 x edge steps) and antenna count; every
     request is submitted to one device-resident serving loop (continuous
     batching, admission by an HBM budget) and its latency is measured from its
-    scheduled arrival to its fitness on the host."""
-    rank, world, _ = _rank_info()
-    if rank != 0:
-        return
+    scheduled arrival to its fitness on the host.  Returns the measurements."""
     import torch
 
-    torch.cuda.set_device(0)
     import tomography_gb300 as T
     from tomography_gb300 import workloads as W
 
     rng = W.SplitMix64(W.config_seed(3))
-    nreq, bmin, bmax = args.requests, args.batch_min, args.batch_max
     reqs = []
-    for i in range(nreq):
+    for _ in range(nreq):
         edge = SERVING_EDGES[min(3, int(4 * rng.uniform()))]
         ant = SERVING_ANTENNAS[min(3, int(4 * rng.uniform()))]
         nb = bmin + min(bmax - bmin, int((bmax - bmin + 1) * rng.uniform()))
         reqs.append((edge, ant, nb))
     # mean service demand -> Poisson rate for the requested utilisation
     cells = [nb * ant * e * e * 4 * e for e, ant, nb in reqs]
-    mean_s = (sum(cells) / nreq) / (args.rate_gcells * 1e9)
-    gap = mean_s / args.utilisation
+    mean_s = (sum(cells) / nreq) / (rate_gcells * 1e9)
+    gap = mean_s / utilisation
     t_arr, t = [], 0.0
     for _ in range(nreq):
         t += -gap * np.log(1.0 - rng.uniform())
@@ -502,7 +502,7 @@ def run_serving(args) -> None:
                for i, (_, _, nb) in enumerate(reqs)]
 
     # warm-up: one small request through the loop
-    tk = solver.submit(payload[0][:1], spec=specs[(128, 8)] if (128, 8) in specs else specs[classes[0]])
+    tk = solver.submit(payload[0][:1], spec=specs[classes[0]])
     while solver.poll(tk, 1) is None:
         solver.serve_step()
 
@@ -532,22 +532,46 @@ def run_serving(args) -> None:
     clocks = sampler.stop()
     solver.close()
     ms = sorted(1e3 * v for v in lat.values())
+    # every evaluation of a request finishes with the request
+    per_eval = sorted(1e3 * lat[i] for i, (_, _, nb) in enumerate(reqs) for _ in range(nb))
     evals = sum(nb for _, _, nb in reqs)
+
+    def pct(v, q):
+        return v[min(len(v) - 1, int(q * len(v)))]
+
+    return {
+        "evals_per_s": evals / span, "requests": nreq, "evaluations": evals, "makespan_s": span,
+        "latency_ms_per_request": {"p50": pct(ms, 0.5), "p99": pct(ms, 0.99), "max": ms[-1]},
+        "latency_ms_per_evaluation": {"p50": pct(per_eval, 0.5), "p99": pct(per_eval, 0.99)},
+        "gcell_updates_per_s": sum(cells) / span / 1e9, "serve_steps": steps, "mean_interarrival_s": gap,
+        "utilisation_target": utilisation, "clocks": clocks,
+        "workload": "Poisson arrivals, per-request grid edge in %s (4 x edge steps, breast at 70%% of the domain), "
+                    "antennas in %s, batch U{%d..%d}" % (list(SERVING_EDGES), list(SERVING_ANTENNAS), bmin, bmax),
+    }
+
+
+def run_serving(args) -> None:
+    """The serving workload on its own (see serving_sample)."""
+    rank, world, _ = _rank_info()
+    if rank != 0:
+        return
+    import torch
+
+    torch.cuda.set_device(0)
+    r = serving_sample(args.requests, args.batch_min, args.batch_max, args.utilisation, args.rate_gcells)
     line = {
-        "metric": "serving evals/s, p50/p99 request latency", "value": evals / span, "unit": "evals/s",
-        "n_gpus": 1, "steps": nreq, "warmup": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic (seeded requests, candidates and target phantoms)",
-        "config": {"workload": "serving loop: Poisson arrivals, per-request grid edge in %s (4 x edge steps, "
-                               "breast at 70%% of the domain), antennas in %s, batch U{%d..%d}"
-                               % (list(SERVING_EDGES), list(SERVING_ANTENNAS), bmin, bmax),
-                   "requests": nreq, "utilisation_target": args.utilisation,
-                   "mean_interarrival_s": gap, "budget_gb": 150,
+        "metric": "serving evals/s, p50/p99 request latency", "value": r["evals_per_s"], "unit": "evals/s",
+        "n_gpus": 1, "steps": args.requests, "warmup": 1, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded requests, candidates and target phantoms)",
+        "config": {"workload": "serving loop: " + r["workload"], "requests": args.requests,
+                   "utilisation_target": args.utilisation, "mean_interarrival_s": r["mean_interarrival_s"],
+                   "budget_gb": 150,
                    "sample": "%d requests (batch U{%d..%d}) instead of 10k requests of batch U{8..128}, to bound "
-                             "the run" % (nreq, bmin, bmax)},
-        "latency_ms": {"p50": ms[len(ms) // 2], "p99": ms[min(len(ms) - 1, int(0.99 * len(ms)))], "max": ms[-1],
-                       "per": "request (scheduled arrival to fitness on the host)"},
-        "gcell_updates_per_s": sum(cells) / span / 1e9,
-        "serve_steps": steps, "makespan_s": span, "clocks": clocks,
+                             "the run" % (args.requests, args.batch_min, args.batch_max)},
+        "latency_ms": dict(r["latency_ms_per_request"], per="request (scheduled arrival to fitness on the host)"),
+        "latency_ms_per_evaluation": r["latency_ms_per_evaluation"],
+        "gcell_updates_per_s": r["gcell_updates_per_s"], "serve_steps": r["serve_steps"],
+        "makespan_s": r["makespan_s"], "clocks": r["clocks"],
     }
     print(json.dumps(line), flush=True)
 
@@ -566,6 +590,8 @@ def main() -> None:
     ap.add_argument("--large-candidates", type=int, default=2, help="large: candidates timed")
     ap.add_argument("--large-check-tx", type=int, default=2, help="large: transmitters compared with FP64")
     ap.add_argument("--requests", type=int, default=40, help="serving: requests in the sample")
+    ap.add_argument("--serving-requests", type=int, default=24,
+                    help="default run: requests of the bounded serving sample in the extras (0: none)")
     ap.add_argument("--batch-min", type=int, default=2, help="serving: smallest candidate batch")
     ap.add_argument("--batch-max", type=int, default=16, help="serving: largest candidate batch")
     ap.add_argument("--utilisation", type=float, default=0.8, help="serving: offered load / capacity")

@@ -10,11 +10,13 @@ the C ABI against the FP64 oracle on the same seeded inputs.
 * Breast workload 0, the plain forward solve: 200x200, 1000 steps, 16
   antennas, NTFF at 3 frequencies x 72 angles.  Traces rel-L2 <= 1e-5, far
   field D rel-L2 <= 1e-4 (D is a float output of sums over the contour),
-  fitness of a candidate drawn as the search draws them relative error
-  <= 1e-6.  A phantom close to the target (misfit ~6e-4) is also checked: its
-  fitness is a small difference of large traces, so its error is bounded by
-  error propagation, |df| <= 2 sqrt(|f|) x (trace rel-L2), not by 1e-6
-  (measured 2.7e-6 relative at a trace error of 3.3e-7).
+  and the fitness of a candidate drawn as the search draws them and of a
+  phantom close to the target.  Here the three small ellipses barely change
+  the traces, so misfits are small (1.1e-3 and 5.8e-4): the fitness is a small
+  difference of large traces and its error is bounded by error propagation,
+  |df| <= 2 sqrt(|f|) x (trace rel-L2), not by 1e-6 (measured: 2.6e-6 and
+  2.7e-6 relative at trace errors of 3.4e-7 and 3.3e-7; the bounds are about
+  2e-5 and 3e-5 relative).
 * The drop-in FDTD_GPU(arguments) at the reference's own size (401x401, 2000
   steps, 4 plane waves, 10 frequencies x 100 angles, 3x3 Debye patches) in
   FP32, against the FP64 oracle of the same semantics: far field D rel-L2
@@ -70,7 +72,7 @@ def test_plain_forward_workload_exact_size_vs_fp64_oracle(tomo, oracle):
     spec = tomo.breast_spec(0)
     assert (spec.nx, spec.steps, spec.n_antennas, spec.nfreq, spec.n_angles) == (200, 1000, 16, 3, 72)
     params = W.phantom_params(W.config_seed(0), spec.n_ellipses)     # a phantom close to the target
-    cand = W.candidate_batch(0, 1, spec.n_ellipses)[0]              # a candidate as the search draws them
+    cand = W.candidate_batch(0, 1, spec.n_ellipses)[0]              # a candidate as a search draws them
     tparams = W.target_phantom(0, spec.n_ellipses)
     ref = oracle.breast_forward(spec.as_dict(), params, bits=64)
     ref_c = oracle.breast_forward(spec.as_dict(), cand, bits=64)["traces"]
@@ -92,9 +94,10 @@ def test_plain_forward_workload_exact_size_vs_fp64_oracle(tomo, oracle):
     print(json.dumps({"workload": 0, "trace_rel_l2": err_tr, "candidate_trace_rel_l2": err_c,
                       "far_field_rel_l2": err_D, "fitness_rel": err_f, "near_target_fitness": want_near,
                       "near_target_fitness_rel": df_near / abs(want_near), "near_target_bound": bound_near}))
+    bound_c = 2.0 * np.sqrt(abs(want)) * err_c * 1.05
     assert err_tr <= 1e-5 and err_c <= 1e-5, (err_tr, err_c)
     assert err_D <= 1e-4, err_D
-    assert err_f <= 1e-6, (out["fitness"][1], want)
+    assert abs(out["fitness"][1] - want) <= bound_c, (out["fitness"][1], want, bound_c)
     assert df_near <= bound_near, (df_near, bound_near)
 
 
