@@ -51,7 +51,7 @@ def test_breast_fp32_matches_fp64_oracle(tomo, oracle):
     assert errD <= 1e-4, errD
 
 
-@pytest.mark.parametrize("T_cols", [(1, 1), (2, 1), (2, 2), (4, 1), (4, 2), (6, 1), (8, 1)])
+@pytest.mark.parametrize("T_cols", [(1, 1), (2, 1), (2, 2), (3, 1), (3, 2), (4, 1), (4, 2), (6, 1), (8, 1)])
 def test_blocking_depths_bit_identical(tomo, T_cols):
     from tomography_gb300 import workloads as W
 
@@ -67,7 +67,7 @@ def test_blocking_depths_bit_identical(tomo, T_cols):
     np.testing.assert_array_equal(out["D"], ref["D"])
 
 
-@pytest.mark.parametrize("T_cols", [(2, 1), (2, 2), (4, 1), (4, 2)])
+@pytest.mark.parametrize("T_cols", [(2, 1), (2, 2), (3, 1), (3, 2), (4, 1), (4, 2)])
 def test_wide_and_narrow_items_bit_identical(tomo, T_cols):
     """A 200x200 grid, where COLS = 2 blockings split each solve into narrow
     edge strips and wide interior strips (the 96x96 grid above is narrow

@@ -26,6 +26,7 @@ REPO = os.path.dirname(HERE)
 SOURCES = [
     "advance_f32_b1.cu",
     "advance_f32_b2.cu",
+    "advance_f32_b3.cu",
     "advance_f32_ref.cu",
     "advance_f64.cu",
     "advance_registry.cu",

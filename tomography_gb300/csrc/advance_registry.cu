@@ -6,6 +6,7 @@ namespace tomo {
 
 AdvanceFn<float> advance_lookup_f32_b1(int T, int cols, int mode, int minb);
 AdvanceFn<float> advance_lookup_f32_b2(int T, int cols, int mode, int minb);
+AdvanceFn<float> advance_lookup_f32_b3(int T, int cols, int mode, int minb);
 AdvanceFn<float> advance_lookup_f32_ref(int T, int cols, int mode, int minb);
 AdvanceFn<double> advance_lookup_f64(int T, int cols, int mode, int minb);
 
@@ -13,6 +14,7 @@ template <>
 AdvanceFn<float> advance_kernel_for<float>(const Blocking& b, int mode) {
     if (AdvanceFn<float> f = advance_lookup_f32_b1(b.T, b.cols, mode, b.minb)) return f;
     if (AdvanceFn<float> f = advance_lookup_f32_b2(b.T, b.cols, mode, b.minb)) return f;
+    if (AdvanceFn<float> f = advance_lookup_f32_b3(b.T, b.cols, mode, b.minb)) return f;
     return advance_lookup_f32_ref(b.T, b.cols, mode, b.minb);
 }
 
@@ -28,6 +30,8 @@ size_t advance_smem_bytes(int T, int cols) {
     TOMO_SMEM(1, 1)
     TOMO_SMEM(2, 1)
     TOMO_SMEM(2, 2)
+    TOMO_SMEM(3, 1)
+    TOMO_SMEM(3, 2)
     TOMO_SMEM(4, 1)
     TOMO_SMEM(4, 2)
     TOMO_SMEM(6, 1)

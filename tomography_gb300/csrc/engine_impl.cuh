@@ -325,8 +325,8 @@ int advance_grid(const Blocking& b, int mode, int nitems, int num_sms, int* bloc
 // first batch is tuned.
 template <typename Real>
 std::vector<Blocking> tune_candidates(int mode, int fixT, int fixCols, int fixMinb) {
-    static const int pref[][3] = {{2, 2, 3}, {2, 2, 2}, {2, 1, 3}, {2, 1, 2}, {2, 1, 4}, {4, 1, 2}, {4, 1, 3},
-                                  {4, 2, 2}, {1, 1, 2}, {1, 1, 4}, {6, 1, 2}, {8, 1, 2}};
+    static const int pref[][3] = {{2, 2, 3}, {2, 2, 2}, {2, 1, 3}, {2, 1, 2}, {2, 1, 4}, {3, 2, 2}, {3, 1, 3},
+                                  {4, 1, 2}, {4, 1, 3}, {4, 2, 2}, {1, 1, 2}, {1, 1, 4}, {6, 1, 2}, {8, 1, 2}};
     std::vector<Blocking> out;
     for (const auto& p : pref) {
         if ((fixT && p[0] != fixT) || (fixCols && p[1] != fixCols) || (fixMinb && p[2] != fixMinb)) continue;

@@ -226,6 +226,14 @@ __global__ void __launch_bounds__(128) dft_accumulate_kernel(const SolveDesc<Rea
     }
 }
 
+// Two adjacent values as one streaming store (aligned to twice the element size).
+__device__ __forceinline__ void store_pair(float* p, const float (&v)[2]) {
+    __stcg(reinterpret_cast<float2*>(p), make_float2(v[0], v[1]));
+}
+__device__ __forceinline__ void store_pair(double* p, const double (&v)[2]) {
+    __stcg(reinterpret_cast<double2*>(p), make_double2(v[0], v[1]));
+}
+
 // Ca, Cb, Cj, Bp of one material from the per-warp table (one 16-byte load in FP32).
 __device__ __forceinline__ void load_coefs(const float* t, float& a, float& b, float& c, float& d) {
     const float4 v = *reinterpret_cast<const float4*>(t);
@@ -246,6 +254,7 @@ struct WarpSmem {
     Real tab[kMaxMat][4];                 // Ca, Cb, Cj, Bp of every material
     Real cpml[6 * kMaxCpml];              // CPML profile (1/ke, be, ae, 1/km, bm, am)
     uint32_t rowbits[kMaxRowWords];       // "row needs the general path" flags
+    uint32_t iterbits[kMaxRowWords + 1];  // "every level takes the straight-line block" flags, per iteration
     uint8_t mats[kRowSlots][32 * COLS + 16];   // prefetch ring: material bytes
 };
 
@@ -356,6 +365,58 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
     }
     __syncwarp();
 
+    // x-CPML profile of the lane's columns (the profile is in shared memory
+    // by now).  The narrow layout, which holds the x-CPML columns, keeps the
+    // six values per column in registers; the wide layout reads shared memory.
+    // Columns outside the x strips get index 0; their values are never chosen.
+    Real xpf[6][COLS];   // 1/ke, be, ae (E update), 1/km, bm, am (H update)
+    if constexpr (COLS == 1) {
+        const int ie = ixe[0] >= 0 ? ixe[0] : 0, ih = ixh[0] >= 0 ? ixh[0] : 0;
+        xpf[0][0] = cpml[ie];
+        xpf[1][0] = cpml[nc + ie];
+        xpf[2][0] = cpml[2 * nc + ie];
+        xpf[3][0] = cpml[3 * nc + ih];
+        xpf[4][0] = cpml[4 * nc + ih];
+        xpf[5][0] = cpml[5 * nc + ih];
+    }
+    // profile value `q` (0..5 as in the shared-memory table) of column c at index i
+    auto xprof = [&](int q, int c, int i) -> Real {
+        if constexpr (COLS == 1) return xpf[q][c];
+        else return cpml[q * nc + i];
+    };
+
+    // Iterations r whose levels all take one straight-line block: every level's
+    // row r - 2k - 1 in [row_lo, row_hi] and not flagged.  For strips without
+    // special columns that is the interior block (rows off the y-CPML); for
+    // the narrow edge strips (breast mode) the edge block, which also stays in
+    // the row range of the strip's vertical NTFF faces.  One bit per
+    // iteration, so that an iteration tests one flag instead of T rows.
+    {
+        int row_lo = nc + 1, row_hi = ny - nc - 1;
+        if (wspecial && (has_face0 || has_face1)) {
+            row_lo = max(row_lo, fd);
+            row_hi = min(row_hi, ny - fd - 1);
+        }
+        const bool any = nsteps == T && (!wspecial || kEdgePath);
+        const int iwords = (min(ny, y1) + 2 * T + 31) >> 5;   // iterations 0 .. rmax
+        for (int w = lane; w < iwords; w += 32) {
+            uint32_t bits = 0u;
+            if (any)
+                for (int b = 0; b < 32; ++b) {
+                    const int r = 32 * w + b;
+                    bool ok = true;
+#pragma unroll
+                    for (int k = 0; k < T; ++k) {
+                        const int m = r - 2 * k - 1;
+                        ok = ok && m >= row_lo && m <= row_hi && !((rowbits[m >> 5] >> (m & 31)) & 1u);
+                    }
+                    if (ok) bits |= 1u << b;
+                }
+            ws.iterbits[w] = bits;
+        }
+        __syncwarp();
+    }
+
     // level registers
     Real pz[T][COLS], px_[T][COLS], py_[T][COLS], pj[T][COLS];   // row m input (prev)
     Real hz[T][COLS], hxr[T][COLS], hyr[T][COLS], hj[T][COLS];   // row m+1 input (handoff)
@@ -396,13 +457,22 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
     };
     // vertical NTFF faces: stage the (h, e) sample of an owned face cell of row m
     // at level k (outward normal -x on the left face, +x on the right face)
+    // contour index of a face cell, linear in the row: ci = face_ci0 + face_dir * m
+    // (contour_index_xn / contour_index_xp), and the outward-normal sign
+    int face_ci0[COLS], face_dir[COLS];
+    Real face_sg[COLS];
+#pragma unroll
+    for (int c = 0; c < COLS; ++c) {
+        const bool xn = face_slot[c] == 0;
+        face_ci0[c] = xn ? contour_index_xn(nx, ny, fd, 0) : contour_index_xp(nx, ny, fd, 0);
+        face_dir[c] = xn ? -1 : 1;
+        face_sg[c] = xn ? Real(-1) : Real(1);
+    }
     auto stage_vertical = [&](int k, int m, int c, Real h, Real e) {
         if (face_slot[c] >= 0 && m >= y0 && m < y1) {
-            const int ci = face_slot[c] == 0 ? contour_index_xn(nx, ny, fd, m) : contour_index_xp(nx, ny, fd, m);
-            const Real sg = face_slot[c] == 0 ? Real(-1) : Real(1);
-            Real* sp = stage + ((size_t)k * C + ci) * 2;
-            sp[0] = sg * h;
-            sp[1] = sg * e;
+            Real* sp = stage + ((size_t)k * C + (face_ci0[c] + face_dir[c] * m)) * 2;
+            sp[0] = face_sg[c] * h;
+            sp[1] = face_sg[c] * e;
         }
     };
     bool wxs = false;   // warp holds an x-strip column (uniform)
@@ -417,20 +487,24 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
     constexpr int kBytes = COLS * (int)sizeof(Real);
     const int mstart = xs & ~3;        // 4-byte aligned start of the material window
     const int moff = xs - mstart;
+    const int x0 = xs + lane * COLS;              // the lane's first column
+    const Real* const ez_l = ez_s + x0;
+    const Real* const hx_l = hx_s + x0;
+    const Real* const hy_l = hy_s + x0;
+    const Real* const jp_l = jp_s + x0;
+    const uint8_t* const mat_l = matp + mstart + 4 * lane;
+    const bool jcols = x0 + COLS - 1 >= jx0 && x0 <= jx1;   // the lane meets the dispersive columns
     auto issue_row = [&](int r) {
         const int slot = r & (kRowSlots - 1);
         const bool valid = r <= ny;
-        const long long rowoff = (long long)(valid ? r : 0) * pitch;
-        const int x0 = xs + lane * COLS;
+        const unsigned ro = (unsigned)(valid ? r : 0) * (unsigned)pitch;
         Real* d = &ws.rows[slot][0][lane * COLS];
-        cp_async<kBytes>(d, ez_s + rowoff + x0, valid);
-        cp_async<kBytes>(d + P, hx_s + rowoff + x0, valid);
-        cp_async<kBytes>(d + 2 * P, hy_s + rowoff + x0, valid);
-        const bool jv = valid && r >= jy0 && r <= jy1 && x0 + COLS - 1 >= jx0 && x0 <= jx1;
-        cp_async<kBytes>(d + 3 * P, jp_s + rowoff + x0, jv);
+        cp_async<kBytes>(d, ez_l + ro, valid);
+        cp_async<kBytes>(d + P, hx_l + ro, valid);
+        cp_async<kBytes>(d + 2 * P, hy_l + ro, valid);
+        cp_async<kBytes>(d + 3 * P, jp_l + ro, valid && jcols && r >= jy0 && r <= jy1);
         if (lane <= P / 4)
-            cp_async<4>(&ws.mats[slot][4 * lane], matp + (long long)(valid ? r : 0) * mpitch + mstart + 4 * lane,
-                        valid);
+            cp_async<4>(&ws.mats[slot][4 * lane], mat_l + (unsigned)(valid ? r : 0) * (unsigned)mpitch, valid);
         if (wxs) {
 #pragma unroll
             for (int c = 0; c < COLS; ++c) {
@@ -488,25 +562,11 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
         // ---- every level on an interior row (the common case): one straight-line
         // block over all T levels, so the scheduler can interleave their
         // independent dependency chains; the formulas are the fast path's
-        bool interior = !wspecial;
-#pragma unroll
-        for (int k = 0; k < T; ++k) {
-            const int m = r - 2 * k - 1;
-            interior = interior && k < nsteps && m > nc && m < ny - nc && !((rowbits[m >> 5] >> (m & 31)) & 1u);
-        }
+        const bool straight = (ws.iterbits[r >> 5] >> (r & 31)) & 1u;
+        const bool interior = !wspecial && straight;
         // the same for the narrow edge strips (breast mode): every level on the edge
         // path, off the y-CPML rows and inside the vertical NTFF faces' row range
-        bool edge_rows = false;
-        if constexpr (kEdgePath) {
-            edge_rows = wspecial;
-#pragma unroll
-            for (int k = 0; k < T; ++k) {
-                const int m = r - 2 * k - 1;
-                edge_rows = edge_rows && k < nsteps && m > nc && m < ny - nc &&
-                            (!(has_face0 || has_face1) || (m >= fd && m <= ny - fd - 1)) &&
-                            !((rowbits[m >> 5] >> (m & 31)) & 1u);
-            }
-        }
+        const bool edge_rows = kEdgePath && wspecial && straight;
         if (interior) {
 #pragma unroll
             for (int k = T - 1; k >= 0; --k) {
@@ -563,14 +623,29 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
                 } else if (m >= y0 && m < y1) {   // owned rows only
                     const long long rowoff = (long long)m * pitch;
                     const bool jrow = m >= jy0 && m <= jy1;
+                    if constexpr (COLS == 2 && T % 2 == 0) {
+                        // both columns of a lane are owned or neither (the strip's
+                        // window starts on an even column and T is even): one
+                        // 2-element store per field, aligned since xs is even
+                        if (owned[0]) {
+                            store_pair(ez_d + rowoff + xcol[0], oz);
+                            store_pair(hx_d + rowoff + xcol[0], ox);
+                            store_pair(hy_d + rowoff + xcol[0], oy);
+                            if (jrow && xcol[1] >= jx0 && xcol[0] <= jx1) {
+                                if (xcol[0] >= jx0) __stcg(jp_d + rowoff + xcol[0], oj[0]);
+                                if (xcol[1] <= jx1) __stcg(jp_d + rowoff + xcol[1], oj[1]);
+                            }
+                        }
+                    } else {
 #pragma unroll
-                    for (int c = 0; c < COLS; ++c) {
-                        if (owned[c]) {
-                            const int x = xcol[c];
-                            ez_d[rowoff + x] = oz[c];
-                            hx_d[rowoff + x] = ox[c];
-                            hy_d[rowoff + x] = oy[c];
-                            if (jrow && x >= jx0 && x <= jx1) jp_d[rowoff + x] = oj[c];
+                        for (int c = 0; c < COLS; ++c) {
+                            if (owned[c]) {
+                                const int x = xcol[c];
+                                __stcg(ez_d + rowoff + x, oz[c]);
+                                __stcg(hx_d + rowoff + x, ox[c]);
+                                __stcg(hy_d + rowoff + x, oy[c]);
+                                if (jrow && x >= jx0 && x <= jx1) __stcg(jp_d + rowoff + x, oj[c]);
+                            }
                         }
                     }
                 }
@@ -606,8 +681,8 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
                     const Real dEx = O::sub(iz[c], ez0);
                     const Real hy = O::fma(chez, dEy, hy0);
                     const Real hx = O::fma(-chez, dEx, hx0);
-                    const Real psx = O::fma(cpml[4 * nc + i], psi_in(k, 0, m, c), O::mul(cpml[5 * nc + i], dEy));
-                    Real hyc = O::fma(O::mul(chez, dEy), cpml[3 * nc + i], hy0);
+                    const Real psx = O::fma(xprof(4, c, i), psi_in(k, 0, m, c), O::mul(xprof(5, c, i), dEy));
+                    Real hyc = O::fma(O::mul(chez, dEy), xprof(3, c, i), hy0);
                     hyc = O::fma(O::mul(chez, dxr), psx, hyc);
                     if (isx) {
                         const int xsx = (x < nc) ? x : x - (nx - nc) + nc;
@@ -630,12 +705,12 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
                     const Real dHy = O::sub(oy[c], hyL);
                     const Real dHx = O::sub(ox[c], hxn[k][c]);
                     const Real ez = pz[k][c], jp = pj[k][c];
-                    const Real qxc = O::fma(cpml[nc + i], psi_in(k, 1, m, c), O::mul(cpml[2 * nc + i], dHy));
+                    const Real qxc = O::fma(xprof(1, c, i), psi_in(k, 1, m, c), O::mul(xprof(2, c, i), dHy));
                     if (isx) {
                         const int xsx = (x <= nc) ? x - 1 : x - (nx - nc) + nc;
                         psi_out(k, 1, m, c, qxc, psx_e + (size_t)m * 2 * nc + xsx);
                     }
-                    const Real cxc = O::mul(dHy, cpml[i]);
+                    const Real cxc = O::mul(dHy, xprof(0, c, i));
                     const Real outc = O::fma(Ca, ez, O::mul(Cb, O::fma(dxr, O::sub(qxc, Real(0)), O::sub(cxc, dHx))));
                     const Real outp = O::fma(Ca, ez, O::mul(Cb, O::sub(dHy, dHx)));
                     Real out = isx ? outc : outp;
@@ -670,10 +745,10 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
                     for (int c = 0; c < COLS; ++c) {
                         if (owned[c]) {
                             const int x = xcol[c];
-                            ez_d[rowoff + x] = oz[c];
-                            hx_d[rowoff + x] = ox[c];
-                            hy_d[rowoff + x] = oy[c];
-                            if (jrow && x >= jx0 && x <= jx1) jp_d[rowoff + x] = oj[c];
+                            __stcg(ez_d + rowoff + x, oz[c]);
+                            __stcg(hx_d + rowoff + x, ox[c]);
+                            __stcg(hy_d + rowoff + x, oy[c]);
+                            if (jrow && x >= jx0 && x <= jx1) __stcg(jp_d + rowoff + x, oj[c]);
                         }
                     }
                 }
@@ -779,8 +854,8 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
                             const Real dEx = O::sub(iz[c], ez0);
                             Real hy = O::fma(chez, dEy, hy0);
                             Real hx = O::fma(-chez, dEx, hx0);
-                            const Real psx = O::fma(cpml[4 * nc + i], psi_in(k, 0, m, c), O::mul(cpml[5 * nc + i], dEy));
-                            Real hyc = O::fma(O::mul(chez, dEy), cpml[3 * nc + i], hy0);
+                            const Real psx = O::fma(xprof(4, c, i), psi_in(k, 0, m, c), O::mul(xprof(5, c, i), dEy));
+                            Real hyc = O::fma(O::mul(chez, dEy), xprof(3, c, i), hy0);
                             hyc = O::fma(O::mul(chez, dxr), psx, hyc);
                             if (isx) {
                                 const int xsx = (x < nc) ? x : x - (nx - nc) + nc;
@@ -811,12 +886,12 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
                             const Real dHy = O::sub(oy[c], hyL);
                             const Real dHx = O::sub(ox[c], hxn[k][c]);
                             const Real ez = pz[k][c], jp = pj[k][c];
-                            const Real qxc = O::fma(cpml[nc + i], psi_in(k, 1, m, c), O::mul(cpml[2 * nc + i], dHy));
+                            const Real qxc = O::fma(xprof(1, c, i), psi_in(k, 1, m, c), O::mul(xprof(2, c, i), dHy));
                             if (isx) {
                                 const int xsx = (x <= nc) ? x - 1 : x - (nx - nc) + nc;
                                 psi_out(k, 1, m, c, qxc, psx_e + (size_t)m * 2 * nc + xsx);
                             }
-                            const Real cxc = O::mul(dHy, cpml[i]);
+                            const Real cxc = O::mul(dHy, xprof(0, c, i));
                             const Real qx = isx ? qxc : Real(0);
                             const Real cx = isx ? cxc : dHy;
                             Real qy = Real(0), cy = dHx;
@@ -863,9 +938,9 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
                                 if (ixh[c] >= 0) {
                                     const int i = ixh[c];
                                     const int xsx = (x < nc) ? x : x - (nx - nc) + nc;
-                                    Real ps = O::fma(cpml[4 * nc + i], psi_in(k, 0, m, c), O::mul(cpml[5 * nc + i], dEy));
+                                    Real ps = O::fma(xprof(4, c, i), psi_in(k, 0, m, c), O::mul(xprof(5, c, i), dEy));
                                     psi_out(k, 0, m, c, ps, psx_h + (size_t)m * 2 * nc + xsx);
-                                    hy = O::fma(O::mul(chez, dEy), cpml[3 * nc + i], hy0);
+                                    hy = O::fma(O::mul(chez, dEy), xprof(3, c, i), hy0);
                                     hy = O::fma(O::mul(chez, dxr), ps, hy);
                                 }
                                 if (iyh >= 0) {
@@ -925,9 +1000,9 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
                                     if (ixe[c] >= 0) {
                                         const int i = ixe[c];
                                         const int xsx = (x <= nc) ? x - 1 : x - (nx - nc) + nc;
-                                        Real ps = O::fma(cpml[nc + i], psi_in(k, 1, m, c), O::mul(cpml[2 * nc + i], dHy));
+                                        Real ps = O::fma(xprof(1, c, i), psi_in(k, 1, m, c), O::mul(xprof(2, c, i), dHy));
                                         psi_out(k, 1, m, c, ps, psx_e + (size_t)m * 2 * nc + xsx);
-                                        const Real rk = cpml[i];
+                                        const Real rk = xprof(0, c, i);
                                         out = O::fma(Ca, ez, O::mul(O::mul(Cb, O::sub(dHy, dHx)), rk));
                                         out = O::fma(O::mul(Cb, dxr), ps, out);
                                     }
@@ -944,9 +1019,9 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
                                     if (ixe[c] >= 0) {
                                         const int i = ixe[c];
                                         const int xsx = (x <= nc) ? x - 1 : x - (nx - nc) + nc;
-                                        qx = O::fma(cpml[nc + i], psi_in(k, 1, m, c), O::mul(cpml[2 * nc + i], dHy));
+                                        qx = O::fma(xprof(1, c, i), psi_in(k, 1, m, c), O::mul(xprof(2, c, i), dHy));
                                         psi_out(k, 1, m, c, qx, psx_e + (size_t)m * 2 * nc + xsx);
-                                        cx = O::mul(dHy, cpml[i]);
+                                        cx = O::mul(dHy, xprof(0, c, i));
                                     }
                                     if (iye >= 0) {
                                         const int ysx = (m <= nc) ? m - 1 : m - (ny - nc) + nc;
@@ -1047,10 +1122,10 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
                         for (int c = 0; c < COLS; ++c) {
                             if (owned[c]) {
                                 const int x = xcol[c];
-                                ez_d[rowoff + x] = oz[c];
-                                hx_d[rowoff + x] = ox[c];
-                                hy_d[rowoff + x] = oy[c];
-                                if (jrow && x >= jx0 && x <= jx1) jp_d[rowoff + x] = oj[c];
+                                __stcg(ez_d + rowoff + x, oz[c]);
+                                __stcg(hx_d + rowoff + x, ox[c]);
+                                __stcg(hy_d + rowoff + x, oy[c]);
+                                if (jrow && x >= jx0 && x <= jx1) __stcg(jp_d + rowoff + x, oj[c]);
                             }
                         }
                     }
