@@ -87,6 +87,13 @@ typedef struct tomo_spec {
     int32_t cols_per_lane;     /* columns per lane; 0: autotuned                     */
     int32_t plain;             /* 1: one solve per launch sequence, one launch per
                                   step, no CUDA graph (the plain baseline path)      */
+    int32_t total_field;       /* 1 (reference GPU mode only): the legacy total-field
+                                  far field of oldFDTD_GPU.cu:425-482,655-717,762-824.
+                                  Each batch also advances one incident vacuum grid
+                                  driven at (nx/2, ny/2) by 100 (-dt/eps0) fwf(n, 0,0,0,0);
+                                  the contour sums take H + H_inc and Ez plus the
+                                  two-level average of Ez_inc, with M at (n - 1/2) dt.
+                                  Not accepted by the serving loop.                  */
 } tomo_spec;
 
 typedef struct tomo_handle tomo_handle;

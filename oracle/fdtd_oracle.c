@@ -126,6 +126,84 @@ static double pw_g(const oracle_problem *p, double t, int x, int y) {
 
 static real nan_clamp(real v) { return isnan(v) ? (real)0 : v; }
 
+/* H update of one grid (FDTD_GPU.cu:298-355; oldFDTD_GPU.cu:425-482 runs the
+   same update on the incident grid) */
+static void h_update(int nx, int ny, int nc, real chez, real dxr, const real *km, const real *bm, const real *am,
+                     int clampnan, const real *Ez, real *Hx, real *Hy, real *phyx, real *phxy) {
+    const int se = nx + 1, sh = nx;
+    for (int y = 0; y < ny; ++y)
+        for (int x = 0; x < nx; ++x) {
+            const size_t h = (size_t)x + (size_t)y * sh, e = (size_t)x + (size_t)y * se;
+            real dEy = Ez[e + 1] - Ez[e];
+            real dEx = Ez[e + se] - Ez[e];
+            real hy = Hy[h] + chez * dEy;
+            real hx = Hx[h] - chez * dEx;
+            int ix = x < nc ? nc - 1 - x : (x >= nx - nc ? x - nx + nc : -1);
+            if (ix >= 0) {
+                hy = Hy[h] + chez * dEy / km[ix];
+                phyx[h] = bm[ix] * phyx[h] + am[ix] * dEy;
+                hy += chez * dxr * phyx[h];
+            }
+            int iy = y < nc ? nc - 1 - y : (y >= ny - nc ? y - ny + nc : -1);
+            if (iy >= 0) {
+                hx = Hx[h] - chez * dEx / km[iy];
+                phxy[h] = bm[iy] * phxy[h] + am[iy] * dEx;
+                hx -= chez * dxr * phxy[h];
+            }
+            if (clampnan) { hx = nan_clamp(hx); hy = nan_clamp(hy); }
+            Hx[h] = hx;
+            Hy[h] = hy;
+        }
+}
+
+/* E update of the incident vacuum grid (oldFDTD_GPU.cu:655-717): Ceze = 1,
+   Cezhy = cb, the source added at (sx, sy) before the CPML strip branches,
+   which overwrite the interior value as written; Ezp keeps the previous level. */
+static void e_update_incident(int nx, int ny, int nc, real cb, real dxr, const real *ke, const real *be,
+                              const real *ae, int sx, int sy, real src, const real *Hx, const real *Hy, real *Ez,
+                              real *Ezp, real *pezx, real *pezy) {
+    const int se = nx + 1, sh = nx;
+    for (int y = 0; y <= ny; ++y)
+        for (int x = 0; x <= nx; ++x) {
+            const size_t e = (size_t)x + (size_t)y * se;
+            real out = 0;
+            if (!(x == 0 || y == 0 || x == nx || y == ny)) {
+                const size_t h = (size_t)x + (size_t)y * sh;
+                real dHy = Hy[h] - Hy[h - 1];
+                real dHx = Hx[h] - Hx[h - sh];
+                real ez = Ez[e];
+                out = ez + cb * dHy - cb * dHx;
+                if (x == sx && y == sy) out = out + src;
+                if (x <= nc) {
+                    int i = nc - x;
+                    out = ez + cb * dHy / ke[i] - cb * dHx / ke[i];
+                    pezx[e] = be[i] * pezx[e] + ae[i] * dHy;
+                    out += cb * dxr * pezx[e];
+                }
+                if (x >= nx - nc) {
+                    int i = x - nx + nc;
+                    out = ez + cb * dHy / ke[i] - cb * dHx / ke[i];
+                    pezx[e] = be[i] * pezx[e] + ae[i] * dHy;
+                    out += cb * dxr * pezx[e];
+                }
+                if (y <= nc) {
+                    int i = nc - y;
+                    out = ez + cb * dHy / ke[i] - cb * dHx / ke[i];
+                    pezy[e] = be[i] * pezy[e] + ae[i] * dHx;
+                    out -= cb * dxr * pezy[e];
+                }
+                if (y >= ny - nc) {
+                    int i = y - ny + nc;
+                    out = ez + cb * dHy / ke[i] - cb * dHx / ke[i];
+                    pezy[e] = be[i] * pezy[e] + ae[i] * dHx;
+                    out -= cb * dxr * pezy[e];
+                }
+            }
+            Ezp[e] = Ez[e];
+            Ez[e] = out;
+        }
+}
+
 int oracle_solve(const oracle_problem *p) {
     const int nx = p->nx, ny = p->ny, nc = p->ncpml, S = p->steps;
     if (nx < 4 || ny < 4 || S < 0 || nc < 0 || 2 * nc >= nx || 2 * nc >= ny || p->nmat < 1 || p->nmat > 128)
@@ -138,8 +216,21 @@ int oracle_solve(const oracle_problem *p) {
     real *phyx = calloc(nH, sizeof(real)), *phxy = calloc(nH, sizeof(real));
     real tab[128][ORACLE_NCOEF];
     real prof[6][64];
-    if (!Ez || !Jp || !Hx || !Hy || !pezx || !pezy || !phyx || !phxy || nc > 64) {
+    const int total = (p->flags & ORACLE_TOTAL_FIELD) != 0;
+    const int mlag = total || (p->flags & ORACLE_M_LAG) != 0;
+    /* incident grid (total field): Ez now / previous level, H, psi */
+    real *Ezi = NULL, *Ezip = NULL, *Hxi = NULL, *Hyi = NULL, *pezxi = NULL, *pezyi = NULL, *phyxi = NULL,
+         *phxyi = NULL;
+    if (total) {
+        Ezi = calloc(nE, sizeof(real)); Ezip = calloc(nE, sizeof(real));
+        pezxi = calloc(nE, sizeof(real)); pezyi = calloc(nE, sizeof(real));
+        Hxi = calloc(nH, sizeof(real)); Hyi = calloc(nH, sizeof(real));
+        phyxi = calloc(nH, sizeof(real)); phxyi = calloc(nH, sizeof(real));
+    }
+    if (!Ez || !Jp || !Hx || !Hy || !pezx || !pezy || !phyx || !phxy || nc > 64 ||
+        (total && (!Ezi || !Ezip || !Hxi || !Hyi || !pezxi || !pezyi || !phyxi || !phxyi || !p->inc_wave))) {
         free(Ez); free(Jp); free(Hx); free(Hy); free(pezx); free(pezy); free(phyx); free(phxy);
+        free(Ezi); free(Ezip); free(Hxi); free(Hyi); free(pezxi); free(pezyi); free(phyxi); free(phxyi);
         return -1;
     }
     for (int m = 0; m < p->nmat; ++m)
@@ -152,32 +243,12 @@ int oracle_solve(const oracle_problem *p) {
     const int pw = (p->flags & ORACLE_PLANE_WAVE) != 0;
     const int C = p->nfreq > 0 ? oracle_contour_size(nx, ny, p->nf_d) : 0;
     if (p->nfreq > 0) memset(p->acc, 0, sizeof(double) * 4 * (size_t)C * p->nfreq);
+    if (total && p->nfreq > 0 && p->inc_acc) memset(p->inc_acc, 0, sizeof(double) * 4 * (size_t)C * p->nfreq);
+    const real cbi = (real)(p->dt / (p->dx * EPS0_D));   /* Cezhy of vacuum */
 
     for (int n = 0; n < S; ++n) {
         /* ---- H update (FDTD_GPU.cu:298-355) */
-        for (int y = 0; y < ny; ++y)
-            for (int x = 0; x < nx; ++x) {
-                const size_t h = (size_t)x + (size_t)y * sh, e = (size_t)x + (size_t)y * se;
-                real dEy = Ez[e + 1] - Ez[e];
-                real dEx = Ez[e + se] - Ez[e];
-                real hy = Hy[h] + chez * dEy;
-                real hx = Hx[h] - chez * dEx;
-                int ix = x < nc ? nc - 1 - x : (x >= nx - nc ? x - nx + nc : -1);
-                if (ix >= 0) {
-                    hy = Hy[h] + chez * dEy / km[ix];
-                    phyx[h] = bm[ix] * phyx[h] + am[ix] * dEy;
-                    hy += chez * dxr * phyx[h];
-                }
-                int iy = y < nc ? nc - 1 - y : (y >= ny - nc ? y - ny + nc : -1);
-                if (iy >= 0) {
-                    hx = Hx[h] - chez * dEx / km[iy];
-                    phxy[h] = bm[iy] * phxy[h] + am[iy] * dEx;
-                    hx -= chez * dxr * phxy[h];
-                }
-                if (clampnan) { hx = nan_clamp(hx); hy = nan_clamp(hy); }
-                Hx[h] = hx;
-                Hy[h] = hy;
-            }
+        h_update(nx, ny, nc, chez, dxr, km, bm, am, clampnan, Ez, Hx, Hy, phyx, phxy);
         /* ---- E update (FDTD_GPU.cu:358-434) */
         for (int y = 0; y <= ny; ++y)
             for (int x = 0; x <= nx; ++x) {
@@ -232,12 +303,28 @@ int oracle_solve(const oracle_problem *p) {
         /* ---- receivers */
         for (int r = 0; r < p->nrx; ++r)
             p->traces[(size_t)r * S + n] = (double)Ez[p->rx[2 * r] + (size_t)p->rx[2 * r + 1] * se];
-        /* ---- running DFT on the contour (FDTD_GPU.cu:231-280) */
+        /* ---- incident grid (total field): H then E, after the main grid
+           (oldFDTD_GPU.cu:425-482, 655-717) */
+        if (total) {
+            h_update(nx, ny, nc, chez, dxr, km, bm, am, clampnan, Ezi, Hxi, Hyi, phyxi, phxyi);
+            e_update_incident(nx, ny, nc, cbi, dxr, ke, be, ae, p->inc_x, p->inc_y, (real)p->inc_wave[n], Hxi, Hyi,
+                              Ezi, Ezip, pezxi, pezyi);
+        }
+        /* ---- running DFT on the contour (FDTD_GPU.cu:231-280; total field
+           oldFDTD_GPU.cu:762-824 with the M phasor at (n - 1/2) dt) */
         for (int f = 0; f < p->nfreq; ++f) {
             double w = 2 * PI_D * p->freqs[f];
+            double tm = mlag ? n - 0.5 : n + 0.5;
             double pjr = cos(w * n * p->dt), pji = -sin(w * n * p->dt);
-            double pmr = cos(w * (n + 0.5) * p->dt), pmi = -sin(w * (n + 0.5) * p->dt);
+            double pmr = cos(w * tm * p->dt), pmi = -sin(w * tm * p->dt);
             double *a = p->acc + (size_t)f * C * 4;
+            /* the incident share alone: M phasor folded over the two levels */
+            double qmr = 0.5 * pmr, qmi = 0.5 * pmi;
+            if (n + 1 < S) {
+                qmr += 0.5 * cos(w * (tm + 1) * p->dt);
+                qmi += -0.5 * sin(w * (tm + 1) * p->dt);
+            }
+            double *ia = (total && p->inc_acc) ? p->inc_acc + (size_t)f * C * 4 : NULL;
             for (int c = 0; c < C; ++c) {
                 int x, y, face;
                 oracle_contour_point(nx, ny, p->nf_d, c, &x, &y, &face);
@@ -248,6 +335,21 @@ int oracle_solve(const oracle_problem *p) {
                 else if (face == 1) { ez = (Ez[e] + Ez[e + 1]) / 2; hv = Hy[h]; s = 1; }
                 else if (face == 2) { ez = (Ez[e + se] + Ez[e]) / 2; hv = Hx[h]; s = -1; }
                 else { ez = (Ez[e] + Ez[e + 1]) / 2; hv = Hy[h]; s = -1; }
+                if (total) {
+                    /* oldFDTD_GPU.cu:781-782, 789-790, 799-800, 808-809 */
+                    const size_t e2 = (face == 0 || face == 2) ? e + se : e + 1;
+                    real hi = (face == 0 || face == 2) ? Hxi[h] : Hyi[h];
+                    real eia = (Ezi[e2] + Ezi[e] + Ezip[e2] + Ezip[e]) / 4;
+                    if (ia) {
+                        double ji = s * (double)hi * p->dt, mi = s * (double)((Ezi[e] + Ezi[e2]) / 2) * p->dt;
+                        ia[4 * c + 0] += ji * pjr;
+                        ia[4 * c + 1] += ji * pji;
+                        ia[4 * c + 2] += mi * qmr;
+                        ia[4 * c + 3] += mi * qmi;
+                    }
+                    ez = ez + eia;
+                    hv = hv + hi;
+                }
                 double jv = s * (double)hv * p->dt, mv = s * (double)ez * p->dt;
                 a[4 * c + 0] += jv * pjr;
                 a[4 * c + 1] += jv * pji;
@@ -261,6 +363,7 @@ int oracle_solve(const oracle_problem *p) {
     if (p->hx_out) for (size_t i = 0; i < nH; ++i) p->hx_out[i] = Hx[i];
     if (p->hy_out) for (size_t i = 0; i < nH; ++i) p->hy_out[i] = Hy[i];
     free(Ez); free(Jp); free(Hx); free(Hy); free(pezx); free(pezy); free(phyx); free(phxy);
+    free(Ezi); free(Ezip); free(Hxi); free(Hyi); free(pezxi); free(pezyi); free(phyxi); free(phxyi);
     return 0;
 }
 

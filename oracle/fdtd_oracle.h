@@ -16,6 +16,8 @@
  *   FDTD_CPU.cxx  the same algorithm on the host (:146-373, :538-614, :893-1479),
  *                 relative misfit :841-845, point-current coefficient :972-983
  *   FDTD_common.cxx  contour index maps :4-46, incident power :48-51
+ *   oldFDTD_GPU.cu   total-field variant: H_inc_update :425-482, E_inc_update
+ *                 :655-717, calculate_JandM_total :762-824
  */
 #ifndef TOMO_FDTD_ORACLE_H
 #define TOMO_FDTD_ORACLE_H
@@ -39,7 +41,12 @@ enum {
 enum {
     ORACLE_REF_CPML = 1,   /* reference E-update strip semantics (FDTD_GPU.cu:389-416) */
     ORACLE_NAN_CLAMP = 2,  /* NaN -> 0 after each update (FDTD_GPU.cu:335-350,425-430) */
-    ORACLE_PLANE_WAVE = 4  /* scattered-field plane-wave source (FDTD_GPU.cu:380-385)  */
+    ORACLE_PLANE_WAVE = 4, /* scattered-field plane-wave source (FDTD_GPU.cu:380-385)  */
+    ORACLE_M_LAG = 8,      /* M phasor at (n - 1/2) dt (oldFDTD_GPU.cu:783,794,805,816)
+                              instead of (n + 1/2) dt (FDTD_GPU.cu:253-276)           */
+    ORACLE_TOTAL_FIELD = 16 /* legacy total-field NTFF (implies ORACLE_M_LAG): an
+                              incident vacuum grid advanced after the main grid each
+                              step, its fields added to the contour samples           */
 };
 
 typedef struct oracle_problem {
@@ -68,6 +75,19 @@ typedef struct oracle_problem {
     double *acc;           /* [nfreq][C][4]: J re, J im, M re, M im          */
     /* optional final state */
     double *ez_out, *hx_out, *hy_out, *jp_out;
+    /* total field (ORACLE_TOTAL_FIELD; oldFDTD_GPU.cu:425-482,655-717,762-824):
+       the incident grid has the main grid's size and CPML, Ceze = 1 and
+       Cezhy = dt/(dx eps0), no Debye current, and inc_wave[n] added to its Ez at
+       (inc_x, inc_y) in step n before the strip overrides (the legacy adds
+       100 Cezj fwf(n) at the grid centre).  The contour samples become
+       H + H_inc and face-avg(Ez) + (face-avg(Ez_inc(n)) + face-avg(Ez_inc(n-1)))/2,
+       summed with J at n dt and M at (n - 1/2) dt.                              */
+    int inc_x, inc_y;
+    const double *inc_wave;   /* [steps] */
+    /* optional: the incident grid's share of acc on its own, with its two-level
+       time average folded into the M phasor: q(n) = (p(n) + p(n+1))/2, p(S) = 0.
+       acc(total) = acc(main grid alone, ORACLE_M_LAG) + inc_acc.               */
+    double *inc_acc;          /* [nfreq][C][4] */
 } oracle_problem;
 
 /* one forward solve; returns 0 on success, -1 on bad input */

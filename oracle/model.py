@@ -29,7 +29,7 @@ EPS0 = 8.85418e-12
 C0 = 1.0 / math.sqrt(MU0 * EPS0)
 ETA0 = math.sqrt(MU0 / EPS0)
 NCOEF = 8
-REF_CPML, NAN_CLAMP, PLANE_WAVE = 1, 2, 4
+REF_CPML, NAN_CLAMP, PLANE_WAVE, M_LAG, TOTAL_FIELD = 1, 2, 4, 8, 16
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -48,6 +48,7 @@ class OracleProblem(C.Structure):
         ("nrx", C.c_int), ("rx", _ip), ("traces", _dp),
         ("nf_d", C.c_int), ("nfreq", C.c_int), ("freqs", _dp), ("acc", _dp),
         ("ez_out", _dp), ("hx_out", _dp), ("hy_out", _dp), ("jp_out", _dp),
+        ("inc_x", C.c_int), ("inc_y", C.c_int), ("inc_wave", _dp), ("inc_acc", _dp),
     ]
 
 
@@ -114,6 +115,16 @@ def source_wave(spec: dict) -> np.ndarray:
     amp = spec["src_amp"] or (2 * spec["bg_eps_inf"] * EPS0 + spec["bg_sigma"] * spec["dt"]) / (2 * spec["dt"])
     t = (np.arange(spec["steps"]) + 0.5) * spec["dt"] - spec["src_t0"]
     return amp * np.sin(2 * PI * spec["src_f0"] * t) * np.exp(-(t / spec["src_tau"]) ** 2)
+
+
+def incident_wave(spec: dict, steps: int | None = None) -> np.ndarray:
+    """Point source of the legacy incident grid, added to its Ez in step n:
+    100 Cezj fwf(n, 0, 0, 0, 0) with Cezj = -dt/eps0 (oldFDTD_GPU.cu:666,682) and
+    fwf at the origin with angle 0 and offset 0: exp(-((n dt - t0)/tau)^2)
+    (oldFDTD_GPU.cu:351-364), t0 and tau of the plane wave."""
+    S = spec["steps"] if steps is None else steps
+    t = np.arange(S) * spec["dt"] - spec["pw_t0"]
+    return 100.0 * (-spec["dt"] / EPS0) * np.exp(-(t / spec["pw_tau"]) ** 2)
 
 
 def material_table_reference(args: np.ndarray, spec: dict) -> tuple[np.ndarray, float]:
@@ -231,6 +242,14 @@ def reference_problem(spec: dict, args: np.ndarray, exc: int, steps: int | None 
     p.pw_t0, p.pw_tau, p.pw_l, p.pw_c0 = spec["pw_t0"], spec["pw_tau"], spec["pw_l"], C0
     if spec["nfreq"] > 0:
         pr.want_dft(spec["nf2ff_d"], spec["freqs"])
+    if spec.get("total_field"):
+        # legacy total-field NTFF: incident grid with the source at the centre
+        # (oldFDTD_GPU.cu:74-75 source_x = nx/2, source_y = ny/2)
+        p.flags |= TOTAL_FIELD
+        p.inc_x, p.inc_y = spec["nx"] // 2, spec["ny"] // 2
+        pr._arr("inc_wave", incident_wave(spec, p.steps))
+        if spec["nfreq"] > 0:
+            pr.inc_acc = pr._arr("inc_acc", np.zeros_like(pr.acc))
     return pr
 
 

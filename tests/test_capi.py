@@ -74,6 +74,10 @@ def test_invalid_specs_are_rejected_before_device_use(tomo):
         tomo.breast_spec(0).copy(antenna_radius=1.0),
         tomo.reference_spec(False).copy(ny=300),
         tomo.breast_spec(0).copy(precision=7),
+        # the total-field variant belongs to the reference GPU mode only
+        tomo.breast_spec(0).copy(total_field=1),
+        tomo.reference_spec(True).copy(total_field=1),
+        tomo.reference_spec(False).copy(total_field=2),
     ]
     for s in bad:
         h = C.c_void_p()

@@ -293,3 +293,54 @@ def test_oracle_fp64_vs_reference_gpu(oracle, case):
         assert abs(want) < 1e-9 and abs(fit) < 1e-9, (fit, want)
     else:
         assert abs(fit - want) <= 1e-5 * abs(want), (fit, want)
+
+
+# ------------------------------------------------------------ total field
+def _total_field_spec() -> dict:
+    """A reduced reference-GPU problem (96x96, 300 steps, 2 plane waves) with
+    the legacy total-field far field of oldFDTD_GPU.cu:425-482,655-717,762-824."""
+    return dict(reference_gpu_spec(), nx=96, ny=96, steps=300, nf2ff_d=20, nfreq=3, freqs=[1e9, 2e9, 3e9],
+                n_angles=16, n_excitations=2, total_field=1)
+
+
+def test_total_field_decomposes_by_linearity(oracle):
+    """The oracle's literal total-field loop (one accumulator of H + H_inc and
+    of face-avg(Ez) + the two-level average of face-avg(Ez_inc), M at
+    (n - 1/2) dt) equals the main grid alone with the lagged M phasor plus the
+    incident grid's own sums with the average folded into its M phasor,
+    q(n) = (p(n) + p(n+1))/2, p(S) = 0 -- the form the product computes."""
+    spec = _total_field_spec()
+    from tomography_gb300 import workloads as W
+
+    args = W.reference_patch_args(77)
+    tf = oracle.reference_problem(spec, args, 1)
+    lag = oracle.reference_problem(dict(spec, total_field=0), args, 1)
+    lag.p.flags |= oracle.M_LAG
+    lead = oracle.reference_problem(dict(spec, total_field=0), args, 1)
+    oracle.run([tf, lag, lead])
+    assert rel_l2(tf.acc, lag.acc + tf.inc_acc) <= 1e-12
+    # both changes matter: the incident grid's share and the half-step lag
+    assert np.linalg.norm(tf.inc_acc) > 0.1 * np.linalg.norm(tf.acc)
+    assert rel_l2(lag.acc, lead.acc) > 1e-3
+
+
+def test_total_field_incident_grid_is_a_centred_point_source(oracle):
+    """The incident grid alone radiates like a point source at the centre of
+    a square grid: at the lowest frequency its far field is isotropic within
+    3% (grid dispersion and the half-cell offset of the contour's centre make
+    the rest), and it does not depend on the candidate or the excitation."""
+    spec = _total_field_spec()
+    from tomography_gb300 import workloads as W
+
+    a = oracle.reference_problem(spec, W.reference_patch_args(78), 0)
+    b = oracle.reference_problem(spec, W.reference_patch_args(79), 1)
+    oracle.run([a, b])
+    np.testing.assert_array_equal(a.inc_acc, b.inc_acc)
+    F, A = 3, 16
+    D = np.zeros((F, A))
+    P = np.zeros((F, A))
+    freqs = np.array(spec["freqs"], dtype=np.float64)
+    oracle.lib().oracle_far_field(96, 96, 20, spec["dx"], F, oracle._d(freqs), oracle._d(np.ascontiguousarray(a.inc_acc)),
+                                  A, 1, spec["pw_tau"], oracle._d(D), oracle._d(P))
+    assert D.min() > 0
+    assert (D[0].max() - D[0].min()) / D[0].mean() <= 0.03

@@ -99,13 +99,17 @@ template <>
 __device__ __forceinline__ void dev_sincos<double>(double a, double* s, double* c) { sincos(a, s, c); }
 
 template <typename Real>
-__global__ void farfield_kernel(const Real* __restrict__ acc, size_t acc_stride, int C, int nfreq,
+__global__ void farfield_kernel(const Real* __restrict__ acc, size_t acc_stride, const Real* __restrict__ inc, int C,
+                                int nfreq,
                                 const double* __restrict__ freqs, const double* __restrict__ geom,
                                 const double* __restrict__ ang, int nang, double dl, int norm, double tau,
                                 float* __restrict__ D, float* __restrict__ P) {
-    // geom[c] = (X, Y, face) [m]; ang[a] = (cos phi, sin phi); sums in Real
+    // geom[c] = (X, Y, face) [m]; ang[a] = (cos phi, sin phi); sums in Real.
+    // inc (total field, may be null): the incident grid's accumulators, added to
+    // every solve's own (the legacy's single sum of both, by linearity).
     const int s = blockIdx.y, f = blockIdx.x;
     const Real* a = acc + (size_t)s * acc_stride + (size_t)f * C * 8;
+    const Real* ia = inc ? inc + (size_t)f * C * 8 : nullptr;
     const double c0 = 1.0 / sqrt(kMu0D * kEps0D), eta0 = sqrt(kMu0D / kEps0D);
     const double fr = freqs[f], k = 2 * kPiD * fr / c0;
     double prad = 1.0;
@@ -123,8 +127,13 @@ __global__ void farfield_kernel(const Real* __restrict__ acc, size_t acc_stride,
             Real sp, cp;
             dev_sincos<Real>(kr * ((Real)g[0] * cphi + (Real)g[1] * sphi), &sp, &cp);
             const Real* e = a + (size_t)c * 8;
-            const Real jr = e[0] - e[2], ji = e[1] - e[3];
-            const Real mr = e[4] - e[6], mi = e[5] - e[7];
+            Real jr = e[0] - e[2], ji = e[1] - e[3];
+            Real mr = e[4] - e[6], mi = e[5] - e[7];
+            if (ia) {
+                const Real* q = ia + (size_t)c * 8;
+                jr += q[0] - q[2]; ji += q[1] - q[3];
+                mr += q[4] - q[6]; mi += q[5] - q[7];
+            }
             const int face = (int)g[2];
             const Real wt = (face == 0 || face == 2) ? -sphi : cphi;
             Nr -= jr * cp - ji * sp;

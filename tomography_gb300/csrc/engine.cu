@@ -204,6 +204,9 @@ int validate_spec(const tomo_spec* s) {
         if (!(s->src_tau > 0)) return fail(TOMO_EINVAL, "src_tau must be positive");
     }
     if (!(s->tau > 0)) return fail(TOMO_EINVAL, "tau must be positive");
+    if (s->total_field != 0 && s->total_field != 1) return fail(TOMO_EINVAL, "total_field must be 0 or 1");
+    if (s->total_field && s->mode != TOMO_MODE_REFERENCE_GPU)
+        return fail(TOMO_EINVAL, "the total-field variant belongs to the reference GPU mode");
     return TOMO_OK;
 }
 
@@ -264,7 +267,9 @@ int build_class(const tomo_spec& s, ProblemClass& pc) {
     pc.pitch = ((kPadLeft + s.nx + 1 + kPadRight) + 31) / 32 * 32;
     pc.mpitch = (kMatPadLeft + s.nx + 1 + 160 + 31) / 32 * 32;
     cpml_profile(s, pc.cpml);
-    // running-DFT phasors (FDTD_GPU.cu:251-276): J at n dt, M at (n + 1/2) dt, times dt
+    // running-DFT phasors (FDTD_GPU.cu:251-276): J at n dt, M at (n + 1/2) dt, times dt;
+    // the total-field variant takes M at (n - 1/2) dt (oldFDTD_GPU.cu:784,794,803,811)
+    const double mshift = s.total_field ? -0.5 : 0.5;
     pc.phasor.assign((size_t)pc.S * std::max(pc.nfreq, 1) * 4, 0.0);
     for (int n = 0; n < pc.S; ++n)
         for (int f = 0; f < pc.nfreq; ++f) {
@@ -272,9 +277,41 @@ int build_class(const tomo_spec& s, ProblemClass& pc) {
             double* p = &pc.phasor[((size_t)n * pc.nfreq + f) * 4];
             p[0] = s.dt * std::cos(w * n * s.dt);
             p[1] = -s.dt * std::sin(w * n * s.dt);
-            p[2] = s.dt * std::cos(w * (n + 0.5) * s.dt);
-            p[3] = -s.dt * std::sin(w * (n + 0.5) * s.dt);
+            p[2] = s.dt * std::cos(w * (n + mshift) * s.dt);
+            p[3] = -s.dt * std::sin(w * (n + mshift) * s.dt);
         }
+    // total field: the legacy sums (H + H_inc) and (Ez + (Ez_inc(n) + Ez_inc(n-1))/2)
+    // in one accumulator.  By linearity that is this class's own sums plus one
+    // incident solve's, whose M phasor absorbs the two-level average:
+    // sum_n e_inc(n) (p(n) + p(n+1))/2 with p(S) = 0.  The incident grid is the
+    // same for every candidate and excitation, so each batch carries one.
+    pc.extra = s.total_field ? 1 : 0;
+    pc.inc_phasor.clear();
+    pc.inc_wave.clear();
+    pc.inc_tab.clear();
+    if (pc.extra) {
+        pc.inc_phasor = pc.phasor;
+        for (int n = 0; n < pc.S; ++n)
+            for (int f = 0; f < pc.nfreq; ++f) {
+                double* q = &pc.inc_phasor[((size_t)n * pc.nfreq + f) * 4];
+                const double* p0 = &pc.phasor[((size_t)n * pc.nfreq + f) * 4];
+                const double* p1 = n + 1 < pc.S ? &pc.phasor[((size_t)(n + 1) * pc.nfreq + f) * 4] : nullptr;
+                q[2] = 0.5 * (p0[2] + (p1 ? p1[2] : 0.0));
+                q[3] = 0.5 * (p0[3] + (p1 ? p1[3] : 0.0));
+            }
+        // E_inc_update (oldFDTD_GPU.cu:655-717): vacuum, Ceze = 1, Cezhy = dt/(dx eps0),
+        // 100 Cezj fwf(n, 0, 0, 0, 0) at the centre, Cezj = -dt/eps0; fwf at the
+        // origin with angle 0 and no offset is exp(-((n dt - t0)/tau)^2)
+        pc.inc_tab.assign((size_t)kMaxMat * kMatCoef, 0.0);
+        pc.inc_tab[kCa] = 1.0;
+        pc.inc_tab[kCb] = s.dt / (s.dx * kEps0D);
+        pc.inc_tab[kCs] = 100.0 * (-s.dt / kEps0D);
+        pc.inc_wave.resize(pc.S);
+        for (int n = 0; n < pc.S; ++n) {
+            const double a = (n * s.dt - s.pw_t0) / s.pw_tau;
+            pc.inc_wave[n] = std::exp(-a * a);
+        }
+    }
     pc.rx.clear();
     pc.patchmap.clear();
     if (s.mode == TOMO_MODE_BREAST) {
@@ -513,6 +550,7 @@ int EngineT<Real>::autotune(size_t ncand) {
     CUDA_TRY(cudaMemsetAsync(d_state_.p, 0, (size_t)nsolves * cd_.lay.per_solve * sizeof(Real), stream_));
     h_descs_.resize(nsolves);
     fill_descs<Real>(cd_, up_, d_state_.as<Real>(), d_mats_.as<uint8_t>(), d_tabs_.as<Real>(), h_descs_.data());
+    if (pc.extra) h_descs_[nsolves - 1] = incident_desc<Real>(cd_, d_state_.as<Real>() + (size_t)(nsolves - 1) * cd_.lay.per_solve);
     double best = 1e300;
     Blocking bestb = cands.front();
     std::vector<WorkItem> items;
@@ -582,7 +620,7 @@ template <typename Real>
 int EngineT<Real>::ensure_batch(int ncand) {
     const ProblemClass& pc = cd_.pc;
     const SolveLayout& L = cd_.lay;
-    const int nsolves = ncand * pc.n_exc;
+    const int nsolves = ncand * pc.n_exc + pc.extra;   // + the total-field incident grid
     const size_t need = (size_t)nsolves * L.per_solve * sizeof(Real);
     if (need > budget_)
         return fail(TOMO_ENOMEM_BUDGET, "batch needs " + std::to_string(need >> 20) + " MiB, budget " +
@@ -680,6 +718,7 @@ int EngineT<Real>::forward(const double* args, size_t ncand, size_t nparam, cons
     CUDA_TRY(cudaMemsetAsync(d_state_.p, 0, (size_t)nsolves * cd_.lay.per_solve * sizeof(Real), stream_));
     h_descs_.resize(nsolves);
     fill_descs<Real>(cd_, up_, d_state_.as<Real>(), d_mats_.as<uint8_t>(), d_tabs_.as<Real>(), h_descs_.data());
+    if (pc.extra) h_descs_[nsolves - 1] = incident_desc<Real>(cd_, d_state_.as<Real>() + (size_t)(nsolves - 1) * cd_.lay.per_solve);
     CUDA_TRY(cudaMemcpyAsync(d_descs_.p, h_descs_.data(), sizeof(SolveDesc<Real>) * nsolves, cudaMemcpyHostToDevice,
                              stream_));
     h2d += sizeof(SolveDesc<Real>) * nsolves;
@@ -709,7 +748,7 @@ int EngineT<Real>::forward(const double* args, size_t ncand, size_t nparam, cons
     CUDA_TRY(cudaMemsetAsync(d_flag_.p, 0, sizeof(int) * 4, stream_));
     float* d_trf = nullptr;
     double* d_trd = nullptr;
-    const size_t ntr = (size_t)pc.nrx * pc.S * nsolves;
+    const size_t ntr = (size_t)pc.nrx * pc.S * (nsolves - pc.extra);
     if (out && out->traces && pc.nrx > 0) {
         TOMO_TRY(d_trf_.ensure(sizeof(float) * ntr));
         d_trf = d_trf_.as<float>();
@@ -720,7 +759,7 @@ int EngineT<Real>::forward(const double* args, size_t ncand, size_t nparam, cons
     }
     TOMO_TRY(post_range<Real>(cd_, ncand, h_descs_[0], want_fit, d_D_.as<float>(), d_P_.as<float>(),
                               d_partials_.as<double>(), d_fit_.as<double>(), d_flag_.as<int>(), d_trf, d_trd, stream_,
-                              &kernels));
+                              &kernels, pc.extra ? h_descs_[nsolves - 1].acc : nullptr));
     if (d_trf) {
         CUDA_TRY(cudaMemcpyAsync(out->traces, d_trf, sizeof(float) * ntr, cudaMemcpyDeviceToHost, stream_));
         d2h += sizeof(float) * ntr;
@@ -730,7 +769,7 @@ int EngineT<Real>::forward(const double* args, size_t ncand, size_t nparam, cons
         d2h += sizeof(double) * ntr;
     }
     if (out && pc.nang > 0) {
-        const size_t n = (size_t)nsolves * pc.nfreq * pc.nang;
+        const size_t n = (size_t)(nsolves - pc.extra) * pc.nfreq * pc.nang;
         if (out->D) {
             CUDA_TRY(cudaMemcpyAsync(out->D, d_D_.p, sizeof(float) * n, cudaMemcpyDeviceToHost, stream_));
             d2h += sizeof(float) * n;

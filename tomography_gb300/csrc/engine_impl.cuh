@@ -81,6 +81,11 @@ struct ProblemClass {
     std::vector<uint8_t> patchmap; // reference modes, (ny+1) x mpitch
     std::vector<double> ffgeom;    // [C][3]: X, Y, face
     std::vector<double> ffang;     // [nang][2]: cos, sin
+    // total-field variant: solves appended to each batch (0 or 1: the incident grid)
+    int extra = 0;
+    std::vector<double> inc_phasor; // [S][nfreq][4]: J at n dt, M folded over two levels
+    std::vector<double> inc_wave;   // [S] incident source waveform
+    std::vector<double> inc_tab;    // [kMaxMat][kMatCoef]: material 0 = vacuum + source coefficient
 };
 
 int validate_spec(const tomo_spec* s);
@@ -124,6 +129,7 @@ struct ClassData {
     ProblemClass pc;
     SolveLayout lay{};
     DevBuf cpml, phasor, wave, rx, patch, freqs, ffgeom, ffang, target;
+    DevBuf inc_phasor, inc_wave, inc_tab, inc_mat;   // total-field incident grid
     bool have_target = false;
 
     int init(const ProblemClass& p) {
@@ -153,6 +159,20 @@ struct ClassData {
         if (pc.nang > 0) {
             TOMO_TRY(ffang.ensure(sizeof(double) * pc.ffang.size()));
             CUDA_TRY(cudaMemcpy(ffang.p, pc.ffang.data(), sizeof(double) * pc.ffang.size(), cudaMemcpyHostToDevice));
+        }
+        if (pc.extra) {
+            auto upload = [](DevBuf& b, const std::vector<double>& v) -> int {
+                std::vector<Real> r(v.begin(), v.end());
+                TOMO_TRY(b.ensure(sizeof(Real) * std::max<size_t>(r.size(), 4)));
+                if (!r.empty()) CUDA_TRY(cudaMemcpy(b.p, r.data(), sizeof(Real) * r.size(), cudaMemcpyHostToDevice));
+                return TOMO_OK;
+            };
+            TOMO_TRY(upload(inc_phasor, pc.inc_phasor));
+            TOMO_TRY(upload(inc_wave, pc.inc_wave));
+            TOMO_TRY(upload(inc_tab, pc.inc_tab));
+            // all-vacuum material map with the patch map's layout
+            TOMO_TRY(inc_mat.ensure(pc.patchmap.size()));
+            CUDA_TRY(cudaMemset(inc_mat.p, 0, pc.patchmap.size()));
         }
         return TOMO_OK;
     }
@@ -261,20 +281,63 @@ void fill_descs(const ClassData<Real>& cd, const Unpacked& u, Real* state_base, 
     }
 }
 
+// Descriptor of the total-field incident grid (oldFDTD_GPU.cu:425-482, 655-717):
+// a reference-mode solve over an all-vacuum map with the legacy centre source,
+// its running DFT against the folded incident phasors.  `state` is one
+// solve's state block (per-solve stride of the class layout).
+template <typename Real>
+SolveDesc<Real> incident_desc(const ClassData<Real>& cd, Real* state) {
+    const ProblemClass& pc = cd.pc;
+    const tomo_spec& s = pc.spec;
+    const SolveLayout& L = cd.lay;
+    SolveDesc<Real> D{};
+    D.nx = s.nx; D.ny = s.ny; D.pitch = pc.pitch; D.mpitch = pc.mpitch;
+    D.ncpml = pc.nc; D.steps_total = pc.S; D.step = 0; D.parity = 0; D.active = 1;
+    D.nrx = 0; D.nf_d = s.nf2ff_d; D.nfreq = pc.nfreq; D.n_contour = pc.C;
+    D.chez = (Real)pc.chez; D.Kp = (Real)pc.Kp; D.dx = (Real)s.dx;
+    Real* f = state + kPadLeft;
+    D.ez[0] = f + 0 * L.field_elems; D.ez[1] = f + 1 * L.field_elems;
+    D.hx[0] = f + 2 * L.field_elems; D.hx[1] = f + 3 * L.field_elems;
+    D.hy[0] = f + 4 * L.field_elems; D.hy[1] = f + 5 * L.field_elems;
+    D.jp[0] = f + 6 * L.field_elems; D.jp[1] = f + 7 * L.field_elems;
+    Real* psib = state + 8 * L.field_elems;
+    D.psi[0] = psib;
+    D.psi[1] = psib + L.psi_elems;
+    D.psi_scratch = psib + 2 * L.psi_elems;
+    D.psi_stride = (int)L.psi_elems;
+    D.traces = psib + (size_t)9 * L.psi_elems;
+    D.acc = D.traces + L.tr_stride;
+    D.stage = D.acc + L.acc_stride;
+    D.mtab = cd.inc_tab.template as<Real>();
+    D.cpml = cd.cpml.template as<Real>();
+    D.src_wave = cd.inc_wave.template as<Real>();
+    D.rx = cd.rx.template as<int>();
+    D.phasor = cd.inc_phasor.template as<Real>();
+    D.jx0 = 1; D.jx1 = 0; D.jy0 = 1; D.jy1 = 0;   // no Debye current anywhere
+    D.dt = s.dt;
+    // the legacy's H_inc_update clamps NaN as the main H update does; the
+    // vacuum grid's fields stay finite, so the flag only keeps the two alike
+    D.flags = kRefCpml | kPointSource | (s.nan_clamp ? kNanClamp : 0);
+    D.mat = cd.inc_mat.template as<uint8_t>() + kMatPadLeft;
+    D.src_x = s.nx / 2;   // oldFDTD_GPU.cu:74-75
+    D.src_y = s.ny / 2;
+    return D;
+}
+
 // Far field + misfit (+ optional traces to float) of a contiguous range of
 // solves whose first descriptor is `first` (host copy).  d_D/d_P hold
 // nsolves*nfreq*nang floats; d_fit receives ncand values.
 template <typename Real>
 int post_range(const ClassData<Real>& cd, size_t ncand, const SolveDesc<Real>& first, bool want_fit, float* d_D,
                float* d_P, double* d_partials, double* d_fit, int* d_flag, float* d_trf, double* d_trd, cudaStream_t st,
-               int64_t* kernels) {
+               int64_t* kernels, const Real* inc_acc = nullptr) {
     const ProblemClass& pc = cd.pc;
     const tomo_spec& s = pc.spec;
     const int nsolves = (int)ncand * pc.n_exc;
     const size_t stride = cd.lay.per_solve;
     if (pc.nang > 0 && pc.C > 0 && d_D) {
         dim3 grd(pc.nfreq, nsolves);
-        farfield_kernel<Real><<<grd, 256, 0, st>>>(first.acc, stride, pc.C, pc.nfreq, cd.freqs.template as<double>(),
+        farfield_kernel<Real><<<grd, 256, 0, st>>>(first.acc, stride, inc_acc, pc.C, pc.nfreq, cd.freqs.template as<double>(),
                                                    cd.ffgeom.template as<double>(), cd.ffang.template as<double>(),
                                                    pc.nang, s.dx, s.ff_norm, s.pw_tau, d_D, d_P);
         ++*kernels;

@@ -291,7 +291,7 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
     const int src = D.parity, dst = 1 - src;
     const Real chez = D.chez, Kp = D.Kp, dxr = D.dx;
     const bool clampnan = kRef && (D.flags & kNanClamp) != 0;
-    const bool psrc = !kRef && (D.flags & kPointSource) != 0;
+    const bool psrc = (D.flags & kPointSource) != 0;
     const int C = D.n_contour, nfreq = D.nfreq, fd = D.nf_d;
     const int psx_h = 0, psx_e = (ny + 1) * 2 * nc;                 // x-strip psi sub-arrays
     const int psy0 = 2 * (ny + 1) * 2 * nc;
@@ -996,6 +996,9 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
                                     out = O::fma(Ca, ez, O::sub(O::mul(Cb, dHy), O::mul(Cb, dHx)));
                                     out = O::fma(cf[kCi], gp, O::fma(cf[kCp], gm, out));
                                     out = O::fma(-Cj, jp, out);
+                                    // total-field incident grid: the legacy centre source, added
+                                    // before the strip overrides (oldFDTD_GPU.cu:680-683)
+                                    if (psrc && m == src_y && x == src_x) out = O::fma(cf[kCs], D.src_wave[n], out);
                                     jpo = O::fma(Kp, jp, O::mul(Bp, O::add(O::sub(out, ez), O::sub(gp, gm))));
                                     if (ixe[c] >= 0) {
                                         const int i = ixe[c];

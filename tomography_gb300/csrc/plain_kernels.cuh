@@ -121,6 +121,8 @@ __global__ void __launch_bounds__(256) plain_e_kernel(const SolveDesc<Real>* __r
         out = O::fma(Ca, ez, O::sub(O::mul(Cb, dHy), O::mul(Cb, dHx)));
         out = O::fma(Ci, gp, O::fma(Cp, gm, out));
         out = O::fma(-Cj, jp, out);
+        // total-field incident grid: the legacy centre source (oldFDTD_GPU.cu:680-683)
+        if ((D.flags & kPointSource) && m == D.src_y && x == D.src_x) out = O::fma(cf[kCs], D.src_wave[n], out);
         jpo = O::fma(Kp, jp, O::mul(Bp, O::add(O::sub(out, ez), O::sub(gp, gm))));
         if (ixe >= 0) {
             const int xsx = (x <= nc) ? x - 1 : x - (nx - nc) + nc;

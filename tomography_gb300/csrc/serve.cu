@@ -117,6 +117,8 @@ template <typename Real>
 static int request_submit(EngineT<Real>* eng, ServeStateT<Real>* st, ClassData<Real>* cd, const double* args,
                           size_t ncand, size_t nparam, uint64_t* ticket) {
     if (!ticket) return fail(TOMO_EINVAL, "ticket is NULL");
+    if (cd->pc.extra)
+        return fail(TOMO_EINVAL, "the total-field variant runs through forward: the serving loop carries no incident grid");
     auto r = std::make_unique<ServeRequest<Real>>();
     TOMO_TRY(unpack_args(cd->pc, args, ncand, nparam, r->up));
     if (!cd->have_target) return fail(TOMO_ENOTARGET, "serving needs a target for this spec");

@@ -63,6 +63,7 @@ class Spec(C.Structure):
         ("steps_per_launch", C.c_int32),
         ("cols_per_lane", C.c_int32),
         ("plain", C.c_int32),
+        ("total_field", C.c_int32),
     ]
 
     def as_dict(self) -> dict:
