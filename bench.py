@@ -73,19 +73,20 @@ def _peaks() -> dict:
 
 def _profile_traffic(T: int, cols: int, minb: int) -> float | None:
     """DRAM bytes per cell-update of the advance kernel from the committed ncu
-    summary, when it was captured with the same blocking."""
+    summary, when it holds a capture with the same blocking (each capture's
+    section opens with its `blocking:` line)."""
     path = os.path.join(REPO, "profiles", "fdtd_advance_pso400.txt")
     if not os.path.exists(path):
         return None
-    value, blocking = None, None
+    found, blocking = {}, None
     for line in open(path):
-        m = re.match(r"\s*dram_bytes_per_cell_update:\s*([0-9.eE+-]+)", line)
-        if m:
-            value = float(m.group(1))
         m = re.match(r"\s*blocking:\s*T=(\d+)\s+COLS=(\d+)\s+MINB=(\d+)", line)
         if m:
             blocking = tuple(int(v) for v in m.groups())
-    return value if blocking == (T, cols, minb) else None
+        m = re.match(r"\s*dram_bytes_per_cell_update:\s*([0-9.eE+-]+)", line)
+        if m and blocking is not None:
+            found[blocking] = float(m.group(1))
+    return found.get((T, cols, minb))
 
 
 class ClockSampler:
@@ -576,6 +577,47 @@ def run_serving(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_plain(args) -> None:
+    """The FP64 plain path on its own: the breast workload's 400x400 grid, one
+    candidate (16 transmitter solves), one solve per launch sequence and one
+    launch per field update and step (H, E, running DFT), no graph.  One
+    untimed forward, then --steps timed forwards; per-step device time is the
+    forward's device time over solves x steps."""
+    rank, world, _ = _rank_info()
+    if rank != 0:
+        return
+    import torch
+
+    torch.cuda.set_device(0)
+    import tomography_gb300 as T
+    from tomography_gb300 import workloads as W
+
+    spec = T.breast_spec(CONFIG_INDEX).copy(precision=T.FP64, plain=1)
+    if args.plain_steps:
+        spec = spec.copy(steps=args.plain_steps)
+    cands = W.candidate_batch(CONFIG_INDEX, 1, spec.n_ellipses)
+    ms = []
+    with T.Solver(spec) as s:
+        s.forward(cands, traces=True, far_field=False)
+        for _ in range(args.steps):
+            s.forward(cands, traces=True, far_field=False)
+            ms.append(s.stats()["total_ms"])
+        st = s.stats()
+    ms.sort()
+    med = ms[len(ms) // 2]
+    nsolve = spec.n_tx
+    line = {
+        "metric": "evals/s (FP64 plain path)", "value": 1e3 / med, "unit": "evals/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": 1, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded candidate)",
+        "config": {"workload": "breast imaging 400x400, %d steps, 1 candidate x %d transmitters, plain FP64 path"
+                               % (spec.steps, nsolve)},
+        "us_per_step": med * 1e3 / (nsolve * spec.steps), "kernels_per_eval": int(st["kernels"]),
+        "gcell_updates_per_s": st["cell_updates"] / (med * 1e6),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -584,7 +626,8 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--candidates", type=int, default=N_CAND)
     ap.add_argument("--no-extras", action="store_true")
-    ap.add_argument("--workload", default="pso", choices=["pso", "serving", "large", "cpu-reference"])
+    ap.add_argument("--workload", default="pso", choices=["pso", "serving", "large", "cpu-reference", "plain"])
+    ap.add_argument("--plain-steps", type=int, default=0, help="plain: override the 3000 steps")
     ap.add_argument("--cpu-steps", type=int, default=2000, help="cpu-reference: steps timed per copy")
     ap.add_argument("--large-steps", type=int, default=0, help="large: override the 20000 steps")
     ap.add_argument("--large-candidates", type=int, default=2, help="large: candidates timed")
@@ -605,6 +648,8 @@ def main() -> None:
         run_serving(args)
     elif args.workload == "large" and args.impl == "ours":
         run_large(args)
+    elif args.workload == "plain" and args.impl == "ours":
+        run_plain(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -185,6 +185,13 @@ int tomo_request_bytes(tomo_handle *h, const tomo_spec *spec, size_t n_cand, uin
 int tomo_serve_step(tomo_handle *h, int *n_active);
 /* fitness of a finished ticket (n_cand values), TOMO_ENOTREADY while running    */
 int tomo_poll(tomo_handle *h, uint64_t ticket, double *fitness);
+/* bounded wait for one ticket: runs tomo_serve_step until the ticket has
+   finished (its result as tomo_poll) or timeout_ms has passed, checked before
+   each step (TOMO_ETIMEOUT; the request stays queued or running and can be
+   waited for again or cancelled).  The caller of a blocking evaluation per
+   request, as tao's workers make one (test.cxx:82-121), uses this instead of
+   its own poll loop.                                                           */
+int tomo_wait(tomo_handle *h, uint64_t ticket, double timeout_ms, double *fitness);
 int tomo_cancel(tomo_handle *h, uint64_t ticket);
 
 /* ---- trace misfit without allocation.  No counterpart in the reference.

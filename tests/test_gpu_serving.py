@@ -160,3 +160,21 @@ def test_cancel(tomo):
         with pytest.raises(tomo.TomoError) as ei:
             s.poll(t2, 2)
         assert ei.value.status == -7   # TOMO_ECANCELLED
+
+
+def test_bounded_wait(tomo):
+    """tomo_wait: a zero timeout on a request nobody has stepped returns
+    TOMO_ETIMEOUT and leaves the request queued; a generous one drives the loop
+    to the batch path's bits."""
+    from tomography_gb300 import workloads as W
+
+    A = _cands(W, 2, 444)
+    with _solver(tomo, W) as s:
+        batch = s.fitness_batch(A)
+        t = s.submit(A)
+        with pytest.raises(tomo.TomoError) as ei:
+            s.wait(t, 2, 0.0)
+        assert ei.value.status == -3
+        assert s.stats()["serve_queued"] == 1
+        got = s.wait(t, 2, 120.0)
+        np.testing.assert_array_equal(got, batch)

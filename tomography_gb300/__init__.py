@@ -109,6 +109,7 @@ def library() -> C.CDLL:
         "tomo_set_target_spec": (I, [P, C.POINTER(Spec), fp, SZ]),
         "tomo_serve_step": (I, [P, C.POINTER(C.c_int)]),
         "tomo_poll": (I, [P, C.c_uint64, dp]),
+        "tomo_wait": (I, [P, C.c_uint64, C.c_double, dp]),
         "tomo_request_bytes": (I, [P, C.c_void_p, SZ, C.POINTER(C.c_uint64)]),
         "tomo_cancel": (I, [P, C.c_uint64]),
         "tomo_get_stats": (I, [P, C.POINTER(Stats)]),
@@ -306,6 +307,14 @@ class Solver:
         if rc == -6:
             return None
         _check(rc)
+        return out
+
+    def wait(self, ticket: int, n_cand: int, timeout_s: float) -> np.ndarray:
+        """Drive the serving loop until `ticket` finishes (its fitness) or
+        `timeout_s` passes (TomoError with status TOMO_ETIMEOUT; the request
+        stays queued or running)."""
+        out = np.zeros(n_cand, dtype=np.float64)
+        _check(library().tomo_wait(self._h, C.c_uint64(ticket), C.c_double(timeout_s * 1e3), _dptr(out)))
         return out
 
     def cancel(self, ticket: int) -> None:

@@ -1,4 +1,5 @@
 // C ABI entry points (include/tomography.h) over the engine.
+#include <chrono>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -104,6 +105,23 @@ int tomo_request_bytes(tomo_handle* h, const tomo_spec* spec, size_t n_cand, uin
 int tomo_poll(tomo_handle* h, uint64_t ticket, double* fitness) {
     if (!h) return fail(TOMO_EINVAL, "NULL handle");
     return h->eng->poll(ticket, fitness);
+}
+
+int tomo_wait(tomo_handle* h, uint64_t ticket, double timeout_ms, double* fitness) {
+    if (!h) return fail(TOMO_EINVAL, "NULL handle");
+    if (!(timeout_ms >= 0)) return fail(TOMO_EINVAL, "tomo_wait: timeout must be >= 0");
+    const auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        const int rc = h->eng->poll(ticket, fitness);
+        if (rc != TOMO_ENOTREADY) return rc;
+        const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (ms >= timeout_ms)
+            return fail(TOMO_ETIMEOUT, "ticket " + std::to_string(ticket) + " not finished after " +
+                                           std::to_string(ms) + " ms");
+        int active = 0;
+        const int st = h->eng->serve_step(&active);
+        if (st != TOMO_OK) return st;
+    }
 }
 
 int tomo_cancel(tomo_handle* h, uint64_t ticket) {
