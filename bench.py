@@ -402,7 +402,7 @@ def run_large(args) -> None:
     """Large-batch workload: 2048x2048 grid, dx 0.125 mm, 16-cell CPML, 20000
     steps, 32 transmitters per candidate, 16 ellipses in a skin-layer disc, NTFF
     at 16 frequencies over 720 angles.  The full 64-candidate batch holds about
-    400 GB of state; this times a bounded subset of candidates (all their
+    340 GB of state; this times a bounded subset of candidates (all their
     transmitters, full steps) and compares FP32 with the FP64 GPU path on the
     first transmitters of one candidate."""
     rank, world, _ = _rank_info()
@@ -444,7 +444,7 @@ def run_large(args) -> None:
         "config": {"workload": "large batch: 2048x2048, dx 0.125 mm, 16-cell CPML, %d steps, 32 tx/candidate, "
                                "16 ellipses, NTFF 16 freqs x 720 angles" % spec.steps,
                    "candidates": ncand, "solves": ncand * spec.n_tx,
-                   "sample": "%d of the 64 candidates (the full batch needs about 400 GB of state)" % ncand,
+                   "sample": "%d of the 64 candidates (the full batch needs about 340 GB of state)" % ncand,
                    "steps_per_launch": st["steps_per_launch"], "cols_per_lane": st["cols_per_lane"],
                    "min_blocks_per_sm": st.get("min_blocks_per_sm")},
         "advance_s": st["advance_ms"] / 1e3, "total_s": st["total_ms"] / 1e3,

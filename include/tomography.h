@@ -229,6 +229,46 @@ int tomo_get_stats(tomo_handle *h, tomo_stats *stats);
    first batch. */
 int tomo_field_snapshot(tomo_handle *h, size_t candidate, int excitation, int field, float *out, size_t n);
 
+/* ---- search drivers: synchronous particle swarm and differential evolution
+   over whole generations, the drop-in for tao's ParticleSwarmMPI /
+   DifferentialEvolutionMPI in the reference's driver (test.cxx:82-121,
+   `ps(min_bound, max_bound, arguments); ps.go(FDTD_GPU)`).  One call of the
+   batch fitness function evaluates a whole generation; fitness is maximised.
+   Host code only: runs without a GPU when the fitness function needs none. */
+enum { TOMO_SEARCH_PS = 0, TOMO_SEARCH_DE = 1 };
+typedef struct tomo_search_params {
+    int32_t type;                 /* TOMO_SEARCH_PS or TOMO_SEARCH_DE                   */
+    int32_t population_size;      /* --population_size (>= 4)                            */
+    int32_t maximum_iterations;   /* --maximum_iterations (generations after the first)  */
+    int32_t number_pairs;         /* DE --number_pairs: difference vectors per donor     */
+    uint64_t seed;                /* --seed                                              */
+    double inertia;               /* PS --inertia                                        */
+    double local_best_weight;     /* PS --local_best_weight                              */
+    double global_best_weight;    /* PS --global_best_weight                             */
+    double crossover_rate;        /* DE --crossover_rate                                 */
+    double differential_scale;    /* DE --differential_scale                             */
+    int32_t parent_best;          /* DE --parent_selection: 1 best, 0 random             */
+    int32_t reserved;
+} tomo_search_params;
+/* fitness[i] of population[i*n_param ...], i < n_cand; non-zero return aborts the search */
+typedef int (*tomo_batch_fitness_fn)(void *user, const double *population, size_t n_cand, size_t n_param,
+                                     double *fitness);
+/* called after every generation with the best fitness and parameters so far */
+typedef void (*tomo_generation_fn)(void *user, int generation, double best_fitness, const double *best_params);
+int tomo_search_defaults(tomo_search_params *p, int type);
+/* tao-style "--name value" arguments over the defaults; unknown names are skipped */
+int tomo_search_parse_args(tomo_search_params *p, int argc, const char *const *argv);
+/* best_params: n_param doubles; history (may be NULL): maximum_iterations + 1
+   best fitness values, the first after the initial generation; evaluations
+   (may be NULL): candidates evaluated */
+int tomo_search_run(const tomo_search_params *p, const double *min_bound, const double *max_bound, size_t n_param,
+                    tomo_batch_fitness_fn f, void *user, tomo_generation_fn report, void *report_user,
+                    double *best_params, double *best_fitness, double *history, int64_t *evaluations);
+/* the same with tomo_fitness_batch of the handle as f (tomo_num_params parameters) */
+int tomo_search_fitness(tomo_handle *h, const tomo_search_params *p, const double *min_bound,
+                        const double *max_bound, tomo_generation_fn report, void *report_user, double *best_params,
+                        double *best_fitness, double *history);
+
 const char *tomo_last_error(void);
 const char *tomo_version(void);
 

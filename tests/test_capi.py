@@ -15,9 +15,14 @@ REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def _declared_functions() -> list[str]:
     names = set()
     for fn in os.listdir(os.path.join(REPO, "include")):
+        # tomography_search.hpp is header-only C++ over the C ABI (its own test
+        # compiles a caller); the other headers declare library symbols
+        if fn == "tomography_search.hpp":
+            continue
         text = open(os.path.join(REPO, "include", fn)).read()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
         text = re.sub(r"//[^\n]*", "", text)
+        text = re.sub(r"typedef\s+[^;{}]*\(\s*\*[^;{}]*;", "", text)   # function-pointer types
         for m in re.finditer(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\([^;{}]*\)\s*;", text):
             name = m.group(1)
             if name not in ("if", "while", "for", "sizeof", "return"):

@@ -12,7 +12,7 @@ CPML, 20000 steps, 32 transmitters, 16 ellipses in a skin-layer disc, NTFF at
   the FP64 GPU path on the same two transmitters: traces rel-L2 <= 1e-5, far
   field rel-L2 <= 1e-4.  The FP64 GPU path is itself held to the oracle by the
   reduced-step check above and the precision study.
-* The full-size state of a 64-candidate batch (about 400 GB) exceeds one GPU;
+* The full-size state of a 64-candidate batch (about 340 GB) exceeds one GPU;
   the batch path rejects it against a memory budget instead of failing in
   cudaMalloc.
 """

@@ -91,3 +91,63 @@ def test_particle_swarm_over_gpu_fitness(tomo):
     assert res.evaluations == 32
     assert np.isfinite(res.best_fitness) and res.best_fitness < 0
     assert all(b >= a for a, b in zip(res.history, res.history[1:]))
+
+
+CPP_PROGRAM = r"""
+#include "tomography_search.hpp"
+#include <cstdio>
+#include <vector>
+
+static double sphere(const std::vector<double>& v) {    // the reference's fitness type
+    double s = 0;
+    for (size_t j = 0; j < v.size(); ++j) s += (v[j] - 0.5 * j) * (v[j] - 0.5 * j);
+    return -s;
+}
+
+int main() {
+    std::vector<double> lo(5, -4.0), hi(5, 4.0);
+    tomo::ParticleSwarm ps(lo, hi, {"--population_size", "30", "--maximum_iterations", "120", "--seed", "7"});
+    int calls = 0;
+    tomo::SearchResult a = ps.go([&](const double* pop, size_t n, size_t np, double* fit) {
+        ++calls;
+        for (size_t i = 0; i < n; ++i) fit[i] = sphere(std::vector<double>(pop + i * np, pop + (i + 1) * np));
+    });
+    tomo::DifferentialEvolution de(lo, hi, {"--population_size", "30", "--maximum_iterations", "150"});
+    tomo::SearchResult b = de.go(sphere);
+    bool threw = false;
+    try {
+        tomo::ParticleSwarm bad(hi, lo);
+        bad.go(sphere);
+    } catch (const std::exception&) {
+        threw = true;
+    }
+    std::printf("%d %lld %zu %.9g %.9g %d\n", calls, (long long)a.evaluations, a.history.size(), a.best_fitness,
+                b.best_fitness, threw ? 1 : 0);
+    return 0;
+}
+"""
+
+
+def test_cpp_drivers_have_the_tao_call_shape(tomo, tmp_path):
+    """A C++ caller constructs the drivers as tao's are constructed in
+    test.cxx:82-121 (bounds, argument strings) and calls go() with a batch
+    lambda or with a function of the reference's fitness type."""
+    import os
+    import shutil
+    import subprocess
+
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    lib_dir = os.path.dirname(tomo.LIB_PATH)
+    src = tmp_path / "search.cpp"
+    src.write_text(CPP_PROGRAM)
+    exe = tmp_path / "search"
+    subprocess.run([cxx, "-std=c++17", "-O1", "-I", os.path.join(repo, "include"), str(src), "-o", str(exe),
+                    "-L", lib_dir, "-ltomography_gb300", "-Wl,-rpath," + lib_dir], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+    calls, evals, nhist = int(out[0]), int(out[1]), int(out[2])
+    assert calls == 121 and evals == 30 * 121 and nhist == 121
+    assert float(out[3]) > -1e-3 and float(out[4]) > -1e-2
+    assert out[5] == "1"   # min > max bounds rejected

@@ -80,6 +80,22 @@ class Stats(C.Structure):
 _lib: Optional[C.CDLL] = None
 
 
+class SearchParams(C.Structure):
+    """Mirror of tomo_search_params (search drivers, tomography_gb300.search)."""
+    _fields_ = [
+        ("type", C.c_int32), ("population_size", C.c_int32), ("maximum_iterations", C.c_int32),
+        ("number_pairs", C.c_int32), ("seed", C.c_uint64),
+        ("inertia", C.c_double), ("local_best_weight", C.c_double), ("global_best_weight", C.c_double),
+        ("crossover_rate", C.c_double), ("differential_scale", C.c_double),
+        ("parent_best", C.c_int32), ("reserved", C.c_int32),
+    ]
+
+
+# tomo_batch_fitness_fn and tomo_generation_fn
+BATCH_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_double), C.c_size_t, C.c_size_t, C.POINTER(C.c_double))
+REPORT_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_double, C.POINTER(C.c_double))
+
+
 def library() -> C.CDLL:
     """Load the native library (raises if it has not been built)."""
     global _lib
@@ -115,6 +131,11 @@ def library() -> C.CDLL:
         "tomo_get_stats": (I, [P, C.POINTER(Stats)]),
         "tomo_field_snapshot": (I, [P, SZ, I, I, fp, SZ]),
         "tomo_trace_misfit_static": (I, [C.c_void_p, C.c_void_p, SZ, SZ, SZ, C.c_void_p, C.c_void_p]),
+        "tomo_search_defaults": (I, [C.POINTER(SearchParams), I]),
+        "tomo_search_parse_args": (I, [C.POINTER(SearchParams), I, C.POINTER(C.c_char_p)]),
+        "tomo_search_run": (I, [C.POINTER(SearchParams), dp, dp, SZ, BATCH_FN, P, REPORT_FN, P, dp, dp, dp,
+                                C.POINTER(C.c_int64)]),
+        "tomo_search_fitness": (I, [P, C.POINTER(SearchParams), dp, dp, REPORT_FN, P, dp, dp, dp]),
         "tomo_last_error": (C.c_char_p, []),
         "tomo_version": (C.c_char_p, []),
         "tomo_fdtd_gpu_set_target": (I, [fp, SZ]),

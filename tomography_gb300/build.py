@@ -33,6 +33,7 @@ SOURCES = [
     "engine.cu",
     "serve.cu",
     "capi.cpp",
+    "search.cpp",
     "fdtd_gpu_dropin.cpp",
     "noalloc.cu",
     "plain.cu",

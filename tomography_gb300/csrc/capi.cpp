@@ -124,6 +124,22 @@ int tomo_wait(tomo_handle* h, uint64_t ticket, double timeout_ms, double* fitnes
     }
 }
 
+// tomo_search_fitness: the search drivers of search.cpp with the handle's
+// batch fitness (tomo_fitness_batch) as the generation evaluator
+static int handle_fitness(void* user, const double* pop, size_t n, size_t np, double* fit) {
+    return tomo_fitness_batch(static_cast<tomo_handle*>(user), pop, n, np, fit);
+}
+
+int tomo_search_fitness(tomo_handle* h, const tomo_search_params* p, const double* min_bound,
+                        const double* max_bound, tomo_generation_fn report, void* report_user, double* best_params,
+                        double* best_fitness, double* history) {
+    if (!h) return fail(TOMO_EINVAL, "NULL handle");
+    const int np = tomo::num_params(&h->spec);
+    if (np < 1) return fail(TOMO_EINVAL, "spec has no parameters");
+    return tomo_search_run(p, min_bound, max_bound, (size_t)np, handle_fitness, h, report, report_user, best_params,
+                           best_fitness, history, nullptr);
+}
+
 int tomo_cancel(tomo_handle* h, uint64_t ticket) {
     if (!h) return fail(TOMO_EINVAL, "NULL handle");
     return h->eng->cancel(ticket);

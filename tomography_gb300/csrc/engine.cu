@@ -757,7 +757,11 @@ int EngineT<Real>::forward(const double* args, size_t ncand, size_t nparam, cons
         TOMO_TRY(d_trd_.ensure(sizeof(double) * ntr));
         d_trd = d_trd_.as<double>();
     }
-    TOMO_TRY(post_range<Real>(cd_, ncand, h_descs_[0], want_fit, d_D_.as<float>(), d_P_.as<float>(),
+    // the far field runs when it is returned or when the misfit needs it (the
+    // reference modes); the breast mode's trace misfit does not
+    const bool want_ff = out && (out->D || out->P || (want_fit && s.mode != TOMO_MODE_BREAST));
+    TOMO_TRY(post_range<Real>(cd_, ncand, h_descs_[0], want_fit, want_ff ? d_D_.as<float>() : nullptr,
+                              want_ff ? d_P_.as<float>() : nullptr,
                               d_partials_.as<double>(), d_fit_.as<double>(), d_flag_.as<int>(), d_trf, d_trd, stream_,
                               &kernels, pc.extra ? h_descs_[nsolves - 1].acc : nullptr));
     if (d_trf) {

@@ -200,7 +200,9 @@ static RequestLayout request_layout(const ClassData<Real>& cd, size_t ncand, siz
     b.mats = pc.spec.mode == TOMO_MODE_BREAST ? align(L.mat_stride * ncand) : 0;
     b.tabs = align(sizeof(Real) * kMaxMat * kMatCoef * ncand);
     b.up = align(sizeof(double) * upload_doubles);
-    b.ff = pc.nang > 0 ? align(sizeof(float) * nsolves * pc.nfreq * pc.nang) : 0;
+    // far field only where the misfit needs it (reference modes); a served
+    // request returns its fitness alone
+    b.ff = pc.nang > 0 && pc.spec.mode != TOMO_MODE_BREAST ? align(sizeof(float) * nsolves * pc.nfreq * pc.nang) : 0;
     b.part = align(sizeof(double) * 2 * nsolves);
     b.fit = align(sizeof(double) * ncand);
     b.total = b.state + b.mats + b.tabs + b.up + 2 * b.ff + b.part + b.fit + 256;

@@ -1,11 +1,13 @@
 """Synchronous particle-swarm and differential-evolution drivers over whole
-generations.
+generations: Python face of the library's C++ drivers (csrc/search.cpp,
+``tomo_search_run`` in include/tomography.h; C++ callers use
+include/tomography_search.hpp).
 
 The reference hands its fitness function to tao's searches as a function
 pointer (test.cxx:82-121): ``ParticleSwarmMPI ps(min_bound, max_bound,
 arguments); ps.go(FDTD_GPU)``, ``DifferentialEvolutionMPI de(...);
 de.go(...)``, with tao farming one candidate per MPI rank and call.  tao itself
-is an un-vendored submodule, so these drivers restate the textbook synchronous
+is an un-vendored submodule, so the drivers restate the textbook synchronous
 algorithms with the same construction and ``go(f)`` call shape, and evaluate
 every generation in ONE call: ``f`` receives the whole population as an
 ``[n, n_param]`` array (``Solver.fitness_batch``), so all candidate x
@@ -23,6 +25,7 @@ Command line (the analogue of the reference's ``--search_type ps|de``)::
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import dataclasses
 import json
 import sys
@@ -32,6 +35,11 @@ from typing import Callable, Sequence
 import numpy as np
 
 FitnessFn = Callable[[np.ndarray], np.ndarray]
+
+SEARCH_PS, SEARCH_DE = 0, 1
+
+
+from . import BATCH_FN, REPORT_FN, SearchParams  # noqa: E402  (ABI mirrors of include/tomography.h)
 
 
 @dataclasses.dataclass
@@ -55,10 +63,12 @@ def get_argument(arguments: Sequence[str] | None, name: str, default, cast=float
 
 
 class _Search:
+    TYPE = SEARCH_PS
+
     def __init__(self, min_bound, max_bound, arguments=None, *, population_size=None, maximum_iterations=None,
                  seed=None):
-        self.lo = np.asarray(min_bound, dtype=np.float64)
-        self.hi = np.asarray(max_bound, dtype=np.float64)
+        self.lo = np.ascontiguousarray(min_bound, dtype=np.float64)
+        self.hi = np.ascontiguousarray(max_bound, dtype=np.float64)
         if self.lo.shape != self.hi.shape or self.lo.ndim != 1:
             raise ValueError("min_bound and max_bound must be equal-length vectors")
         if np.any(self.hi < self.lo):
@@ -68,15 +78,17 @@ class _Search:
         self.maximum_iterations = int(maximum_iterations or get_argument(arguments, "--maximum_iterations", 100, int))
         if self.population_size < 4:
             raise ValueError("population_size must be at least 4")
-        seed = seed if seed is not None else get_argument(arguments, "--seed", 0x70F00001, int)
-        self.rng = np.random.Generator(np.random.PCG64(seed))
-        self.span = self.hi - self.lo
+        self.seed = int(seed if seed is not None else get_argument(arguments, "--seed", 0x70F00001, int))
 
-    def _uniform(self, n: int) -> np.ndarray:
-        return self.lo + self.rng.random((n, self.n_param)) * self.span
+    def _params(self) -> SearchParams:
+        from . import library
 
-    def _clip(self, x: np.ndarray) -> np.ndarray:
-        return np.clip(x, self.lo, self.hi)
+        p = SearchParams()
+        _check_status(library().tomo_search_defaults(C.byref(p), self.TYPE))
+        p.population_size = self.population_size
+        p.maximum_iterations = self.maximum_iterations
+        p.seed = self.seed & 0xFFFFFFFFFFFFFFFF
+        return p
 
     @staticmethod
     def _evaluator(f, batch: bool) -> FitnessFn:
@@ -89,6 +101,54 @@ class _Search:
             return ev
         return lambda x: np.array([float(f(list(row))) for row in x], dtype=np.float64)
 
+    def go(self, f, batch: bool = True, callback=None) -> SearchResult:
+        """Run the search; ``f`` evaluates a whole generation (``batch=True``)
+        or one candidate given as a list (``batch=False``)."""
+        from . import library
+
+        ev = self._evaluator(f, batch)
+        errors = []
+
+        def batch_fn(_user, pop, n, npar, out):
+            try:
+                x = np.ctypeslib.as_array(pop, shape=(n, npar)).copy()
+                np.ctypeslib.as_array(out, shape=(n,))[:] = ev(x)
+                return 0
+            except BaseException as e:   # re-raised after the C driver returns
+                errors.append(e)
+                return -1
+
+        def report_fn(_user, gen, best, params):
+            if callback and not errors:
+                try:
+                    callback(gen, best, np.ctypeslib.as_array(params, shape=(self.n_param,)).copy())
+                except BaseException as e:
+                    errors.append(e)
+
+        cb, rep = BATCH_FN(batch_fn), REPORT_FN(report_fn)
+        p = self._params()
+        best = np.zeros(self.n_param)
+        fit = C.c_double()
+        hist = np.zeros(self.maximum_iterations + 1)
+        evals = C.c_int64()
+        dp = C.POINTER(C.c_double)
+        t0 = time.perf_counter()
+        rc = library().tomo_search_run(C.byref(p), self.lo.ctypes.data_as(dp), self.hi.ctypes.data_as(dp),
+                                       self.n_param, cb, None, rep, None, best.ctypes.data_as(dp), C.byref(fit),
+                                       hist.ctypes.data_as(dp), C.byref(evals))
+        if errors:
+            raise errors[0]
+        _check_status(rc)
+        return SearchResult(float(fit.value), best, [float(h) for h in hist], int(evals.value),
+                            self.maximum_iterations, time.perf_counter() - t0)
+
+
+def _check_status(rc: int) -> None:
+    if rc != 0:
+        from . import _check
+
+        _check(rc)
+
 
 class ParticleSwarm(_Search):
     """Synchronous global-best particle swarm.
@@ -96,6 +156,8 @@ class ParticleSwarm(_Search):
     v <- w v + c1 r1 (p_best - x) + c2 r2 (g_best - x);  x <- clip(x + v).
     ``--inertia``, ``--local_best_weight``, ``--global_best_weight`` as in tao's
     particle swarm arguments."""
+
+    TYPE = SEARCH_PS
 
     def __init__(self, min_bound, max_bound, arguments=None, *, inertia=None, local_best_weight=None,
                  global_best_weight=None, **kw):
@@ -106,35 +168,10 @@ class ParticleSwarm(_Search):
         self.c2 = float(global_best_weight if global_best_weight is not None
                         else get_argument(arguments, "--global_best_weight", 1.5))
 
-    def go(self, f, batch: bool = True, callback=None) -> SearchResult:
-        ev = self._evaluator(f, batch)
-        t0 = time.perf_counter()
-        n = self.population_size
-        x = self._uniform(n)
-        v = (self.rng.random((n, self.n_param)) * 2.0 - 1.0) * self.span * 0.1
-        fx = ev(x)
-        pbest, pfit = x.copy(), fx.copy()
-        g = int(np.argmax(pfit))
-        gbest, gfit = pbest[g].copy(), float(pfit[g])
-        history = [gfit]
-        evals = n
-        for it in range(self.maximum_iterations):
-            r1 = self.rng.random((n, self.n_param))
-            r2 = self.rng.random((n, self.n_param))
-            v = self.inertia * v + self.c1 * r1 * (pbest - x) + self.c2 * r2 * (gbest - x)
-            x = self._clip(x + v)
-            fx = ev(x)
-            evals += n
-            better = fx > pfit
-            pbest[better] = x[better]
-            pfit[better] = fx[better]
-            g = int(np.argmax(pfit))
-            if pfit[g] > gfit:
-                gbest, gfit = pbest[g].copy(), float(pfit[g])
-            history.append(gfit)
-            if callback:
-                callback(it, gfit, gbest)
-        return SearchResult(gfit, gbest, history, evals, self.maximum_iterations, time.perf_counter() - t0)
+    def _params(self) -> SearchParams:
+        p = super()._params()
+        p.inertia, p.local_best_weight, p.global_best_weight = self.inertia, self.c1, self.c2
+        return p
 
 
 class DifferentialEvolution(_Search):
@@ -143,6 +180,8 @@ class DifferentialEvolution(_Search):
     Donor = parent + F * sum_k (x_a_k - x_b_k) over ``--number_pairs`` pairs of
     distinct other members; binomial crossover at ``--crossover_rate`` with at
     least one donor gene; the trial replaces its target when it is not worse."""
+
+    TYPE = SEARCH_DE
 
     def __init__(self, min_bound, max_bound, arguments=None, *, crossover_rate=None, differential_scale=None,
                  number_pairs=None, parent_selection=None, **kw):
@@ -159,39 +198,11 @@ class DifferentialEvolution(_Search):
         if self.population_size < 2 * self.pairs + 2:
             raise ValueError("population too small for the number of difference pairs")
 
-    def go(self, f, batch: bool = True, callback=None) -> SearchResult:
-        ev = self._evaluator(f, batch)
-        t0 = time.perf_counter()
-        n, p = self.population_size, self.n_param
-        x = self._uniform(n)
-        fx = ev(x)
-        history = [float(fx.max())]
-        evals = n
-        for it in range(self.maximum_iterations):
-            best = int(np.argmax(fx))
-            trial = np.empty_like(x)
-            for i in range(n):
-                others = [j for j in range(n) if j != i]
-                pick = self.rng.choice(others, size=2 * self.pairs, replace=False)
-                base = x[best] if self.parent == "best" else x[int(self.rng.choice(others))]
-                donor = base.copy()
-                for k in range(self.pairs):
-                    donor += self.F * (x[pick[2 * k]] - x[pick[2 * k + 1]])
-                mask = self.rng.random(p) < self.cr
-                mask[self.rng.integers(p)] = True
-                trial[i] = np.where(mask, donor, x[i])
-            trial = self._clip(trial)
-            ft = ev(trial)
-            evals += n
-            keep = ft >= fx
-            x[keep] = trial[keep]
-            fx[keep] = ft[keep]
-            history.append(float(fx.max()))
-            if callback:
-                callback(it, history[-1], x[int(np.argmax(fx))])
-        b = int(np.argmax(fx))
-        return SearchResult(float(fx[b]), x[b].copy(), history, evals, self.maximum_iterations,
-                            time.perf_counter() - t0)
+    def _params(self) -> SearchParams:
+        p = super()._params()
+        p.crossover_rate, p.differential_scale, p.number_pairs = self.cr, self.F, self.pairs
+        p.parent_best = 1 if self.parent == "best" else 0
+        return p
 
 
 def breast_bounds(n_ellipses: int, disc_radius: float):
