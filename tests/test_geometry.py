@@ -22,7 +22,7 @@ def _items(lib, nx, nc, d, T, cols, ny=None, nseg=1):
     return [tuple(buf[5 * i + j] for j in range(5)) for i in range(n)]
 
 
-@pytest.mark.parametrize("T,cols", [(1, 1), (2, 1), (2, 2), (3, 1), (3, 2), (4, 1), (4, 2), (6, 1), (8, 1)])
+@pytest.mark.parametrize("T,cols", [(1, 1), (2, 1), (2, 2), (2, 4), (3, 1), (3, 2), (4, 1), (4, 2), (6, 1), (8, 1)])
 def test_strip_geometry(tomo, T, cols):
     lib = tomo.library()
     grids = list(range(16, 140, 3)) + [200, 255, 256, 257, 400, 401, 512, 600, 601, 1024, 2048]

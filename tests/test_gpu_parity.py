@@ -51,7 +51,7 @@ def test_breast_fp32_matches_fp64_oracle(tomo, oracle):
     assert errD <= 1e-4, errD
 
 
-@pytest.mark.parametrize("T_cols", [(1, 1), (2, 1), (2, 2), (3, 1), (3, 2), (4, 1), (4, 2), (6, 1), (8, 1)])
+@pytest.mark.parametrize("T_cols", [(1, 1), (2, 1), (2, 2), (2, 4), (3, 1), (3, 2), (4, 1), (4, 2), (6, 1), (8, 1)])
 def test_blocking_depths_bit_identical(tomo, T_cols):
     from tomography_gb300 import workloads as W
 
@@ -67,7 +67,7 @@ def test_blocking_depths_bit_identical(tomo, T_cols):
     np.testing.assert_array_equal(out["D"], ref["D"])
 
 
-@pytest.mark.parametrize("T_cols", [(2, 1), (2, 2), (3, 1), (3, 2), (4, 1), (4, 2)])
+@pytest.mark.parametrize("T_cols", [(2, 1), (2, 2), (2, 4), (3, 1), (3, 2), (4, 1), (4, 2)])
 def test_wide_and_narrow_items_bit_identical(tomo, T_cols):
     """A 200x200 grid, where COLS = 2 blockings split each solve into narrow
     edge strips and wide interior strips (the 96x96 grid above is narrow
@@ -84,6 +84,30 @@ def test_wide_and_narrow_items_bit_identical(tomo, T_cols):
     np.testing.assert_array_equal(out["traces"], ref["traces"])
     np.testing.assert_array_equal(out["D"], ref["D"])
     assert np.abs(ref["traces"]).max() > 0
+
+
+@pytest.mark.parametrize("blocking", [(4, 2, 2), (3, 2, 2), (2, 4, 2), (2, 2, 3), (2, 2, 2)])
+def test_every_wide_variant_bit_identical(tomo, blocking, monkeypatch):
+    """Each compiled wide variant (T, COLS, minimum resident blocks per SM,
+    fixed through TOMO_T / TOMO_COLS / TOMO_MINB) on the 200x200 grid, which
+    has narrow edge strips and wide interior strips: the bits of one step
+    per launch, one column per lane."""
+    from tomography_gb300 import workloads as W
+
+    T, cols, minb = blocking
+    base = tomo.breast_spec(0).copy(steps=301, n_tx=2)
+    params = W.phantom_params(W.config_seed(0) + 5, base.n_ellipses)
+    with tomo.Solver(base.copy(steps_per_launch=1, cols_per_lane=1)) as s:
+        ref = s.forward(params, traces=True, far_field=True)
+    monkeypatch.setenv("TOMO_T", str(T))
+    monkeypatch.setenv("TOMO_COLS", str(cols))
+    monkeypatch.setenv("TOMO_MINB", str(minb))
+    with tomo.Solver(base) as s:
+        out = s.forward(params, traces=True, far_field=True)
+        st = s.stats()
+    assert (st["steps_per_launch"], st["cols_per_lane"], st["min_blocks_per_sm"]) == blocking
+    np.testing.assert_array_equal(out["traces"], ref["traces"])
+    np.testing.assert_array_equal(out["D"], ref["D"])
 
 
 @pytest.mark.parametrize("nseg", [5, 13])

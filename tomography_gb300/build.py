@@ -27,6 +27,7 @@ SOURCES = [
     "advance_f32_b1.cu",
     "advance_f32_b2.cu",
     "advance_f32_b3.cu",
+    "advance_f32_b4.cu",
     "advance_f32_ref.cu",
     "advance_f64.cu",
     "advance_registry.cu",

@@ -7,6 +7,7 @@ namespace tomo {
 AdvanceFn<float> advance_lookup_f32_b1(int T, int cols, int mode, int minb);
 AdvanceFn<float> advance_lookup_f32_b2(int T, int cols, int mode, int minb);
 AdvanceFn<float> advance_lookup_f32_b3(int T, int cols, int mode, int minb);
+AdvanceFn<float> advance_lookup_f32_b4(int T, int cols, int mode, int minb);
 AdvanceFn<float> advance_lookup_f32_ref(int T, int cols, int mode, int minb);
 AdvanceFn<double> advance_lookup_f64(int T, int cols, int mode, int minb);
 
@@ -15,6 +16,7 @@ AdvanceFn<float> advance_kernel_for<float>(const Blocking& b, int mode) {
     if (AdvanceFn<float> f = advance_lookup_f32_b1(b.T, b.cols, mode, b.minb)) return f;
     if (AdvanceFn<float> f = advance_lookup_f32_b2(b.T, b.cols, mode, b.minb)) return f;
     if (AdvanceFn<float> f = advance_lookup_f32_b3(b.T, b.cols, mode, b.minb)) return f;
+    if (AdvanceFn<float> f = advance_lookup_f32_b4(b.T, b.cols, mode, b.minb)) return f;
     return advance_lookup_f32_ref(b.T, b.cols, mode, b.minb);
 }
 
@@ -30,6 +32,7 @@ size_t advance_smem_bytes(int T, int cols) {
     TOMO_SMEM(1, 1)
     TOMO_SMEM(2, 1)
     TOMO_SMEM(2, 2)
+    TOMO_SMEM(2, 4)
     TOMO_SMEM(3, 1)
     TOMO_SMEM(3, 2)
     TOMO_SMEM(4, 1)

@@ -560,7 +560,7 @@ int EngineT<Real>::autotune(size_t ncand) {
             (long)nsolves * items_per_solve(pc.nx, pc.ny, pc.nc, item_face_distance(pc), c.T, c.cols), pc.ny, c.T,
             24L * num_sms_);
         append_items(items, 0, nsolves, pc.nx, pc.ny, pc.nc, item_face_distance(pc), c.T, c.cols, nseg);
-        TOMO_TRY(validate_items(items, 0, pc.nx, pc.ny, c.T, c.cols));
+        TOMO_TRY(validate_items(items, 0, pc.nx, pc.ny, pc.nc, item_face_distance(pc), c.T, c.cols));
         TOMO_TRY(d_tune_items_.ensure(sizeof(WorkItem) * items.size()));
         CUDA_TRY(cudaMemcpyAsync(d_tune_items_.p, items.data(), sizeof(WorkItem) * items.size(), cudaMemcpyHostToDevice,
                                  stream_));
@@ -646,7 +646,7 @@ int EngineT<Real>::ensure_batch(int ncand) {
         (long)nsolves * items_per_solve(pc.nx, pc.ny, pc.nc, item_face_distance(pc), blk_.T, blk_.cols), pc.ny,
         blk_.T, 24L * num_sms_);
     append_items(items, 0, nsolves, pc.nx, pc.ny, pc.nc, item_face_distance(pc), blk_.T, blk_.cols, nseg);
-    TOMO_TRY(validate_items(items, 0, pc.nx, pc.ny, blk_.T, blk_.cols));
+    TOMO_TRY(validate_items(items, 0, pc.nx, pc.ny, pc.nc, item_face_distance(pc), blk_.T, blk_.cols));
     if (nsolves != nsolves_ || (int)items.size() != nitems_ || ncand != cur_cand_ || blk_.T != items_blk_.T ||
         blk_.cols != items_blk_.cols) {
         invalidate_graph();
@@ -868,7 +868,7 @@ extern "C" int tomo_internal_work_items(int nx, int ny, int ncpml, int d, int T,
                                         int cap) {
     std::vector<tomo::WorkItem> items;
     tomo::append_items(items, 0, 1, nx, ny, ncpml, d, T, cols, nseg);
-    TOMO_TRY(tomo::validate_items(items, 0, nx, ny, T, cols));
+    TOMO_TRY(tomo::validate_items(items, 0, nx, ny, ncpml, d, T, cols));
     if (!out || (int)items.size() > cap) return tomo::fail(TOMO_EINVAL, "item buffer too small");
     for (size_t i = 0; i < items.size(); ++i) {
         const tomo::WorkItem& w = items[i];

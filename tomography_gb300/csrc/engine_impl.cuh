@@ -389,7 +389,8 @@ int advance_grid(const Blocking& b, int mode, int nitems, int num_sms, int* bloc
 template <typename Real>
 std::vector<Blocking> tune_candidates(int mode, int fixT, int fixCols, int fixMinb) {
     static const int pref[][3] = {{2, 2, 3}, {2, 2, 2}, {2, 1, 3}, {2, 1, 2}, {2, 1, 4}, {3, 2, 2}, {3, 1, 3},
-                                  {4, 1, 2}, {4, 1, 3}, {4, 2, 2}, {1, 1, 2}, {1, 1, 4}, {6, 1, 2}, {8, 1, 2}};
+                                  {4, 1, 2}, {4, 1, 3}, {4, 2, 2}, {2, 4, 2}, {1, 1, 2}, {1, 1, 4}, {6, 1, 2},
+                                  {8, 1, 2}};
     std::vector<Blocking> out;
     for (const auto& p : pref) {
         if ((fixT && p[0] != fixT) || (fixCols && p[1] != fixCols) || (fixMinb && p[2] != fixMinb)) continue;
@@ -505,15 +506,23 @@ inline int choose_segments(long strips, int ny, int T, long min_items) {
 // grid and no wider than the layout allows, column windows inside the zero
 // padding of the field rows, and wide windows aligned for COLS-element copies.
 // A violation is a geometry bug; it fails the call instead of launching.
-inline int validate_items(const std::vector<WorkItem>& items, size_t first_item, int nx, int ny, int T, int cols) {
+inline int validate_items(const std::vector<WorkItem>& items, size_t first_item, int nx, int ny, int ncpml, int d,
+                          int T, int cols) {
     for (size_t i = first_item; i < items.size(); ++i) {
         const WorkItem& w = items[i];
         const int c = (cols > 1 && !w.narrow) ? cols : 1;
         const int P = 32 * c;
         const int xs = w.x1 + T - P;
-        if (w.x0 < 0 || w.x1 > nx + 1 || w.x1 <= w.x0 || w.x1 - w.x0 > P - 2 * T || xs > w.x0 - T ||
-            xs < -kPadLeft || xs + P > nx + 1 + kPadRight || (xs % c) != 0 || w.y0 < 0 || w.y1 > ny + 1 ||
-            w.y1 <= w.y0)
+        bool bad = w.x0 < 0 || w.x1 > nx + 1 || w.x1 <= w.x0 || w.x1 - w.x0 > P - 2 * T || xs > w.x0 - T ||
+                   xs < -kPadLeft || xs + P > nx + 1 + kPadRight || (xs % c) != 0 || w.y0 < 0 || w.y1 > ny + 1 ||
+                   w.y1 <= w.y0;
+        // the wide layout treats every column of its window as interior: no PEC
+        // boundary, CPML or vertical NTFF-face column inside it
+        if (c > 1) {
+            bad = bad || xs <= ncpml || xs + P - 1 >= nx - ncpml;
+            if (d >= 0) bad = bad || (d >= xs && d < xs + P) || (nx - d - 1 >= xs && nx - d - 1 < xs + P);
+        }
+        if (bad)
             return fail(TOMO_ECUDA, "internal error: work item (" + std::to_string(w.x0) + ", " + std::to_string(w.x1) +
                                         ") invalid for nx " + std::to_string(nx));
     }

@@ -233,6 +233,14 @@ __device__ __forceinline__ void store_pair(float* p, const float (&v)[2]) {
 __device__ __forceinline__ void store_pair(double* p, const double (&v)[2]) {
     __stcg(reinterpret_cast<double2*>(p), make_double2(v[0], v[1]));
 }
+// Four adjacent floats as one streaming 16-byte store (aligned to 16 bytes).
+__device__ __forceinline__ void store_quad(float* p, const float (&v)[4]) {
+    __stcg(reinterpret_cast<float4*>(p), make_float4(v[0], v[1], v[2], v[3]));
+}
+__device__ __forceinline__ void store_quad(double* p, const double (&v)[4]) {
+    __stcg(reinterpret_cast<double2*>(p), make_double2(v[0], v[1]));
+    __stcg(reinterpret_cast<double2*>(p) + 1, make_double2(v[2], v[3]));
+}
 
 // Ca, Cb, Cj, Bp of one material from the per-warp table (one 16-byte load in FP32).
 __device__ __forceinline__ void load_coefs(const float* t, float& a, float& b, float& c, float& d) {
@@ -248,15 +256,27 @@ __device__ __forceinline__ void load_coefs(const double* t, double& a, double& b
 // the larger of the narrow and the wide layout).
 template <typename Real, int T, int COLS>
 struct WarpSmem {
+    // CPML psi sub-arrays held: hyx, ezx (x strips), hxy, ezy (y strips).  The
+    // wide layout (COLS > 1) never holds an x-strip column, so it keeps the
+    // y-strip pair only (see psi_slot).
+    static constexpr int kPsiF = COLS == 1 ? 4 : 2;
     Real rows[kRowSlots][4][32 * COLS];   // prefetch ring: Ez, Hx, Hy, Jp of kRowSlots rows
-    Real psring[kRowSlots][4][32 * COLS]; // prefetch ring: CPML psi (hyx, ezx, hxy, ezy) at time n0
-    Real pslev[T > 1 ? T - 1 : 1][4][4][32 * COLS];   // psi after level k, 4 rows in flight
+    Real psring[kRowSlots][kPsiF][32 * COLS];   // prefetch ring: CPML psi at time n0
+    Real pslev[T > 1 ? T - 1 : 1][kPsiF][4][32 * COLS];   // psi after level k, 4 rows in flight
     Real tab[kMaxMat][4];                 // Ca, Cb, Cj, Bp of every material
     Real cpml[6 * kMaxCpml];              // CPML profile (1/ke, be, ae, 1/km, bm, am)
     uint32_t rowbits[kMaxRowWords];       // "row needs the general path" flags
     uint32_t iterbits[kMaxRowWords + 1];  // "every level takes the straight-line block" flags, per iteration
     uint8_t mats[kRowSlots][32 * COLS + 16];   // prefetch ring: material bytes
 };
+
+// Slot of psi sub-array f (0 hyx, 1 ezx, 2 hxy, 3 ezy) in a layout's rings; the
+// x-strip sub-arrays of the wide layout are never touched (slot 0 for them is
+// only a placeholder in code that does not run).
+template <int COLS>
+__host__ __device__ constexpr int psi_slot(int f) {
+    return COLS == 1 ? f : (f >= 2 ? f - 2 : 0);
+}
 
 template <typename Real, int T, int COLS>
 constexpr size_t warp_smem_bytes() {
@@ -311,32 +331,42 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
     int ixh[COLS], ixe[COLS];
     bool owned[COLS];
     int face_slot[COLS];   // 0: xn face column, 1: xp face column, -1 none
+    // The wide layout (COLS > 1) never holds a special column: the host puts
+    // the PEC boundary, CPML and vertical NTFF-face columns, and the halo that
+    // reaches them, into narrow items and checks every wide window before
+    // launch (validate_items).  There the column state below is constant and
+    // its code paths drop out of the wide instance.
+    constexpr bool kWide = COLS > 1;
     bool wspecial = false, wdisp = false;
 #pragma unroll
     for (int c = 0; c < COLS; ++c) {
         int x = xs + lane * COLS + c;
         xcol[c] = x;
         owned[c] = x >= ox0 && x < ox1;
-        ixh[c] = (x >= 0 && x < nc) ? nc - 1 - x : ((x >= nx - nc && x < nx) ? x - nx + nc : -1);
-        ixe[c] = (x >= 1 && x <= nc) ? nc - x : ((x >= nx - nc && x <= nx - 1) ? x - nx + nc : -1);
-        face_slot[c] = -1;
-        if (nfreq > 0 && owned[c]) {
-            if (x == fd) face_slot[c] = 0;
-            else if (x == nx - fd - 1) face_slot[c] = 1;
+        ixh[c] = ixe[c] = face_slot[c] = -1;
+        if constexpr (!kWide) {
+            ixh[c] = (x >= 0 && x < nc) ? nc - 1 - x : ((x >= nx - nc && x < nx) ? x - nx + nc : -1);
+            ixe[c] = (x >= 1 && x <= nc) ? nc - x : ((x >= nx - nc && x <= nx - 1) ? x - nx + nc : -1);
+            if (nfreq > 0 && owned[c]) {
+                if (x == fd) face_slot[c] = 0;
+                else if (x == nx - fd - 1) face_slot[c] = 1;
+            }
+            // CPML strips, PEC boundary and padding columns, vertical NTFF faces
+            wspecial |= x <= nc || x >= nx - nc || (nfreq > 0 && (x == fd || x == nx - fd - 1));
         }
-        // CPML strips, PEC boundary and padding columns, vertical NTFF faces
-        wspecial |= x <= nc || x >= nx - nc || (nfreq > 0 && (x == fd || x == nx - fd - 1));
         wdisp |= x >= jx0 && x <= jx1;
     }
     bool has_face0 = false, has_face1 = false;
+    if constexpr (!kWide) {
 #pragma unroll
-    for (int c = 0; c < COLS; ++c) {
-        has_face0 |= face_slot[c] == 0;
-        has_face1 |= face_slot[c] == 1;
+        for (int c = 0; c < COLS; ++c) {
+            has_face0 |= face_slot[c] == 0;
+            has_face1 |= face_slot[c] == 1;
+        }
+        has_face0 = __any_sync(0xffffffffu, has_face0);
+        has_face1 = __any_sync(0xffffffffu, has_face1);
+        wspecial = __any_sync(0xffffffffu, wspecial);
     }
-    has_face0 = __any_sync(0xffffffffu, has_face0);
-    has_face1 = __any_sync(0xffffffffu, has_face1);
-    wspecial = __any_sync(0xffffffffu, wspecial);
     wdisp = __any_sync(0xffffffffu, wdisp);
 
     // rows that need the general path: CPML rows and boundaries, NTFF face rows,
@@ -448,11 +478,11 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
     const Real* __restrict__ psi_src = D.psi[src];
     Real* __restrict__ psi_dst = D.psi[dst];
     auto psi_in = [&](int k, int f, int m, int c) -> Real {
-        if (k == 0) return ws.psring[m & (kRowSlots - 1)][f][lane * COLS + c];
-        return ws.pslev[(k - 1) % (T > 1 ? T - 1 : 1)][f][m & 3][lane * COLS + c];
+        if (k == 0) return ws.psring[m & (kRowSlots - 1)][psi_slot<COLS>(f)][lane * COLS + c];
+        return ws.pslev[(k - 1) % (T > 1 ? T - 1 : 1)][psi_slot<COLS>(f)][m & 3][lane * COLS + c];
     };
     auto psi_out = [&](int k, int f, int m, int c, Real v, size_t goff) {
-        if (k + 1 < T) ws.pslev[k % (T > 1 ? T - 1 : 1)][f][m & 3][lane * COLS + c] = v;
+        if (k + 1 < T) ws.pslev[k % (T > 1 ? T - 1 : 1)][psi_slot<COLS>(f)][m & 3][lane * COLS + c] = v;
         else if (owned[c] && m >= y0 && m < y1) psi_dst[goff] = v;
     };
     // vertical NTFF faces: stage the (h, e) sample of an owned face cell of row m
@@ -475,10 +505,12 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
             sp[1] = face_sg[c] * e;
         }
     };
-    bool wxs = false;   // warp holds an x-strip column (uniform)
+    bool wxs = false;   // warp holds an x-strip column (uniform; never in the wide layout)
+    if constexpr (!kWide) {
 #pragma unroll
-    for (int c = 0; c < COLS; ++c) wxs |= ixh[c] >= 0 || ixe[c] >= 0;
-    wxs = __any_sync(0xffffffffu, wxs);
+        for (int c = 0; c < COLS; ++c) wxs |= ixh[c] >= 0 || ixe[c] >= 0;
+        wxs = __any_sync(0xffffffffu, wxs);
+    }
 
     // Rows stream through a per-warp shared-memory ring: row r + kPrefetch is
     // requested (cp.async) while row r is consumed, so kPrefetch rows of every
@@ -513,9 +545,9 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
                 const bool ev = valid && ixe[c] >= 0 && r >= 1 && r <= ny - 1;
                 const int xh = (x < nc) ? x : x - (nx - nc) + nc;
                 const int xe = (x <= nc) ? x - 1 : x - (nx - nc) + nc;
-                cp_async<sizeof(Real)>(&ws.psring[slot][0][lane * COLS + c],
+                cp_async<sizeof(Real)>(&ws.psring[slot][psi_slot<COLS>(0)][lane * COLS + c],
                                        psi_src + (hv ? psx_h + (size_t)r * 2 * nc + xh : 0), hv);
-                cp_async<sizeof(Real)>(&ws.psring[slot][1][lane * COLS + c],
+                cp_async<sizeof(Real)>(&ws.psring[slot][psi_slot<COLS>(1)][lane * COLS + c],
                                        psi_src + (ev ? psx_e + (size_t)r * 2 * nc + xe : 0), ev);
             }
         }
@@ -527,9 +559,9 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
                 const int x = xcol[c];
                 const bool hv = yh >= 0 && x >= 0 && x < nx;
                 const bool ev = ye >= 0 && x >= 1 && x <= nx - 1;
-                cp_async<sizeof(Real)>(&ws.psring[slot][2][lane * COLS + c],
+                cp_async<sizeof(Real)>(&ws.psring[slot][psi_slot<COLS>(2)][lane * COLS + c],
                                        psi_src + (hv ? psy_h + (size_t)yh * (nx + 1) + x : 0), hv);
-                cp_async<sizeof(Real)>(&ws.psring[slot][3][lane * COLS + c],
+                cp_async<sizeof(Real)>(&ws.psring[slot][psi_slot<COLS>(3)][lane * COLS + c],
                                        psi_src + (ev ? psy_e + (size_t)ye * (nx + 1) + x : 0), ev);
             }
         }
@@ -635,6 +667,27 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
                                 if (xcol[0] >= jx0) __stcg(jp_d + rowoff + xcol[0], oj[0]);
                                 if (xcol[1] <= jx1) __stcg(jp_d + rowoff + xcol[1], oj[1]);
                             }
+                        }
+                    } else if constexpr (COLS == 4) {
+                        // a lane's four columns start on a multiple of 4 (16-byte aligned):
+                        // one store per field where all four are owned, else per column
+                        if (owned[0] && owned[3]) {
+                            store_quad(ez_d + rowoff + xcol[0], oz);
+                            store_quad(hx_d + rowoff + xcol[0], ox);
+                            store_quad(hy_d + rowoff + xcol[0], oy);
+                        } else {
+#pragma unroll
+                            for (int c = 0; c < COLS; ++c)
+                                if (owned[c]) {
+                                    __stcg(ez_d + rowoff + xcol[c], oz[c]);
+                                    __stcg(hx_d + rowoff + xcol[c], ox[c]);
+                                    __stcg(hy_d + rowoff + xcol[c], oy[c]);
+                                }
+                        }
+                        if (jrow) {
+#pragma unroll
+                            for (int c = 0; c < COLS; ++c)
+                                if (owned[c] && xcol[c] >= jx0 && xcol[c] <= jx1) __stcg(jp_d + rowoff + xcol[c], oj[c]);
                         }
                     } else {
 #pragma unroll

@@ -360,7 +360,7 @@ int EngineT<Real>::serve_step(int* n_active) {
             const ProblemClass& pc = r.cd->pc;
             append_items(items, r.first, r.nsolves, pc.nx, pc.ny, pc.nc, item_face_distance(pc), st->blk.T,
                          st->blk.cols, nseg);
-            TOMO_TRY(validate_items(items, n0, pc.nx, pc.ny, st->blk.T, st->blk.cols));
+            TOMO_TRY(validate_items(items, n0, pc.nx, pc.ny, pc.nc, item_face_distance(pc), st->blk.T, st->blk.cols));
             st->cmax = std::max(st->cmax, dft_contour(pc));
         }
         st->nitems = (int)items.size();
