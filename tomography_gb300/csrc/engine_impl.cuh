@@ -493,12 +493,14 @@ inline int items_per_solve(int nx, int ny, int ncpml, int d, int T, int cols) {
 }
 
 // Row segments per strip: 1 while a batch's strips fill the GPU, else enough
-// to reach about min_items items, keeping segments at least 8T and 32 rows
-// tall (each segment recomputes 2T halo rows).  TOMO_SEGMENTS fixes the count.
+// to reach about min_items items, keeping segments at least 6T and 12 rows
+// tall (each segment recomputes 2T halo rows; a sweep of one 4-solve call of
+// 401 rows ran fastest at about 32 segments per strip, 12-13 rows each).
+// TOMO_SEGMENTS fixes the count.
 inline int choose_segments(long strips, int ny, int T, long min_items) {
     if (const char* e = std::getenv("TOMO_SEGMENTS")) return std::max(1, std::atoi(e));
     if (strips <= 0 || strips >= min_items) return 1;
-    const int max_seg = std::max(1, (ny + 1) / std::max(32, 8 * T));
+    const int max_seg = std::max(1, (ny + 1) / std::max(12, 6 * T));
     return (int)std::max(1L, std::min<long>(max_seg, (min_items + strips - 1) / strips));
 }
 
