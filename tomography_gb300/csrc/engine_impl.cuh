@@ -234,7 +234,7 @@ void fill_descs(const ClassData<Real>& cd, const Unpacked& u, Real* state_base, 
         SolveDesc<Real> D{};
         Real* sb = state_base + (size_t)sv * L.per_solve;
         D.nx = s.nx; D.ny = s.ny; D.pitch = pc.pitch; D.mpitch = pc.mpitch;
-        D.ncpml = pc.nc; D.steps_total = pc.S; D.step = 0; D.parity = 0; D.active = 1;
+        D.ncpml = pc.nc; D.steps_total = pc.S; D.step = 0; D.parity = 0; D.active = 1; D.nmat = pc.nmat;
         D.nrx = pc.nrx; D.nf_d = s.nf2ff_d; D.nfreq = pc.nfreq; D.n_contour = pc.C;
         D.chez = (Real)pc.chez; D.Kp = (Real)pc.Kp; D.dx = (Real)s.dx;
         Real* f = sb + kPadLeft;
@@ -292,7 +292,7 @@ SolveDesc<Real> incident_desc(const ClassData<Real>& cd, Real* state) {
     const SolveLayout& L = cd.lay;
     SolveDesc<Real> D{};
     D.nx = s.nx; D.ny = s.ny; D.pitch = pc.pitch; D.mpitch = pc.mpitch;
-    D.ncpml = pc.nc; D.steps_total = pc.S; D.step = 0; D.parity = 0; D.active = 1;
+    D.ncpml = pc.nc; D.steps_total = pc.S; D.step = 0; D.parity = 0; D.active = 1; D.nmat = 1;
     D.nrx = 0; D.nf_d = s.nf2ff_d; D.nfreq = pc.nfreq; D.n_contour = pc.C;
     D.chez = (Real)pc.chez; D.Kp = (Real)pc.Kp; D.dx = (Real)s.dx;
     Real* f = state + kPadLeft;

@@ -322,8 +322,9 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
     const int mpitch = D.mpitch, jx0 = D.jx0, jx1 = D.jx1, jy0 = D.jy0, jy1 = D.jy1;
     const int src_x = D.src_x, src_y = D.src_y;
 
-    // hot material coefficients and the CPML profile -> shared memory (per warp)
-    for (int i = lane; i < kMaxMat * 4; i += 32) ws.tab[i >> 2][i & 3] = D.mtab[(i >> 2) * kMatCoef + (i & 3)];
+    // hot material coefficients (of the solve's materials) and the CPML profile
+    // -> shared memory (per warp)
+    for (int i = lane; i < D.nmat * 4; i += 32) ws.tab[i >> 2][i & 3] = D.mtab[(i >> 2) * kMatCoef + (i & 3)];
     for (int i = lane; i < 6 * nc; i += 32) cpml[i] = D.cpml[i];
 
     // per-column constants
@@ -372,10 +373,17 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
     // rows that need the general path: CPML rows and boundaries, NTFF face rows,
     // plane-wave rows (reference modes), and -- only in the strips whose columns
     // (halo included) hold them -- the source row and receiver rows
+    // Only the words the sweep reads are built: iterations [sweep_r0, sweep_r1]
+    // advance rows down to 2T - 1 below the first (a short row segment needs a
+    // few words, not the whole grid's).
+    const int sweep_r0 = max(0, y0 - 2 * T);           // halo rows below the segment
+    const int sweep_r1 = min(ny, y1) + 2 * T - 1;      // every level advances row y1 (or ny)
+    const int iw_lo = sweep_r0 >> 5, iw_hi = sweep_r1 >> 5;
     uint32_t* rowbits = ws.rowbits;
     const int nwords = (ny + 1 + 31) >> 5;
+    const int rw_lo = max(0, 32 * iw_lo - 2 * T - 1) >> 5, rw_hi = min(nwords - 1, iw_hi);
     const bool src_here = psrc && src_x >= xs && src_x < xs + P;
-    for (int w = lane; w < nwords; w += 32) {
+    for (int w = rw_lo + lane; w <= rw_hi; w += 32) {
         uint32_t bits = 0;
         for (int b = 0; b < 32; ++b) {
             const int m = 32 * w + b;
@@ -428,8 +436,7 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
             row_hi = min(row_hi, ny - fd - 1);
         }
         const bool any = nsteps == T && (!wspecial || kEdgePath);
-        const int iwords = (min(ny, y1) + 2 * T + 31) >> 5;   // iterations 0 .. rmax
-        for (int w = lane; w < iwords; w += 32) {
+        for (int w = iw_lo + lane; w <= iw_hi; w += 32) {
             uint32_t bits = 0u;
             if (any)
                 for (int b = 0; b < 32; ++b) {
@@ -567,8 +574,7 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
         }
         cp_async_commit();
     };
-    const int rstart = max(0, y0 - 2 * T);          // halo rows below the segment
-    const int rmax = min(ny, y1) + 2 * T - 1;         // every level advances row y1 (or ny)
+    const int rstart = sweep_r0, rmax = sweep_r1;
 #pragma unroll 1
     for (int r = rstart; r < rstart + kPrefetch; ++r) issue_row(r);
 

@@ -51,6 +51,7 @@ struct SolveDesc {
     int jx0, jx1, jy0, jy1;      // dispersive bounding box (Jp may be non-zero only inside)
     int psi_stride;              // elements per psi time copy
     int active;                  // 0: skip this solve
+    int nmat;                    // materials in use: indices 0 .. nmat-1 of mtab
     Real chez;                   // dt/(mu0 dx)
     Real Kp;                     // Debye recursion coefficient
     Real dx;
