@@ -93,6 +93,68 @@ def test_particle_swarm_over_gpu_fitness(tomo):
     assert all(b >= a for a, b in zip(res.history, res.history[1:]))
 
 
+@pytest.mark.gpu
+def test_search_fitness_over_a_handle(tomo):
+    """tomo_search_fitness: the C drivers with the handle's tomo_fitness_batch
+    as the generation evaluator.  Same seed, same search as the Python face
+    over Solver.fitness_batch; the reported best re-evaluates to its fitness."""
+    import ctypes as C
+
+    from helpers import small_breast_spec, small_params
+    from tomography_gb300 import workloads as W
+
+    spec = small_breast_spec(tomo, n_ellipses=2)
+    with tomo.Solver(spec.copy(n_ellipses=3)) as ts:
+        target = ts.forward(small_params(W, 3), traces=True, far_field=False)["traces"][0]
+    lo, hi = S.breast_bounds(2, spec.disc_radius)
+    lib = tomo.library()
+    p = tomo.SearchParams()
+    assert lib.tomo_search_defaults(C.byref(p), S.SEARCH_DE) == 0
+    p.population_size, p.maximum_iterations, p.seed = 8, 3, 5
+    best = np.zeros(lo.size)
+    fit = C.c_double()
+    hist = np.zeros(4)
+    dp = C.POINTER(C.c_double)
+    with tomo.Solver(spec) as s:
+        s.set_target(target)
+        rc = lib.tomo_search_fitness(s._h, C.byref(p), lo.ctypes.data_as(dp), hi.ctypes.data_as(dp), tomo.REPORT_FN(), None,
+                                     best.ctypes.data_as(dp), C.byref(fit), hist.ctypes.data_as(dp))
+        assert rc == 0, lib.tomo_last_error()
+        again = s.fitness(best)
+        py = S.DifferentialEvolution(lo, hi, population_size=8, maximum_iterations=3, seed=5).go(s.fitness_batch)
+    assert again == fit.value
+    assert py.best_fitness == fit.value and list(hist) == py.history
+    assert np.all(best >= lo) and np.all(best <= hi)
+
+
+def test_search_argument_errors(tomo):
+    """tao-style arguments: unknown names are skipped, a malformed value or an
+    unknown parent selection is refused; bounds with min > max are refused."""
+    import ctypes as C
+
+    lib = tomo.library()
+    p = tomo.SearchParams()
+    assert lib.tomo_search_defaults(C.byref(p), S.SEARCH_PS) == 0
+    assert lib.tomo_search_defaults(C.byref(p), 7) == -1
+
+    def parse(*argv):
+        arr = (C.c_char_p * len(argv))(*[a.encode() for a in argv])
+        return lib.tomo_search_parse_args(C.byref(p), len(argv), arr)
+
+    assert parse("--population_size", "12", "--unknown", "3", "--inertia", "0.25") == 0
+    assert (p.population_size, p.inertia) == (12, 0.25)
+    assert parse("--population_size", "12x") == -1
+    assert parse("--parent_selection", "worst") == -1
+    assert parse("--parent_selection", "random") == 0 and p.parent_best == 0
+    lo, hi = np.zeros(2), np.ones(2)
+    dp = C.POINTER(C.c_double)
+    best, fit = np.zeros(2), C.c_double()
+    cb = tomo.BATCH_FN(lambda u, pop, n, npar, out: 0)
+    rc = lib.tomo_search_run(C.byref(p), hi.ctypes.data_as(dp), lo.ctypes.data_as(dp), 2, cb, None, tomo.REPORT_FN(), None,
+                             best.ctypes.data_as(dp), C.byref(fit), None, None)
+    assert rc == -1
+
+
 CPP_PROGRAM = r"""
 #include "tomography_search.hpp"
 #include <cstdio>
