@@ -385,7 +385,7 @@ SolveLayout solve_layout(const ProblemClass& pc, size_t real_bytes) {
     L.acc_stride = std::max<size_t>((size_t)pc.nfreq * pc.C * 8, 8);
     L.acc_stride = (L.acc_stride + 31) / 32 * 32;
     const int tmax = 8;
-    L.stage_stride = pc.nfreq > 0 ? ((size_t)tmax * pc.C * 2 + 31) / 32 * 32 : 32;
+    L.stage_stride = pc.nfreq > 0 ? ((size_t)kStageLevels * pc.C * 2 + 31) / 32 * 32 : 32;
     L.per_solve = 8 * L.field_elems + (size_t)(tmax + 1) * L.psi_elems + L.tr_stride + L.acc_stride + L.stage_stride;
     L.per_solve = (L.per_solve + 63) / 64 * 64;
     L.mat_stride = rows * pc.mpitch;
@@ -671,10 +671,17 @@ int EngineT<Real>::build_graph(int nlaunch) {
     TOMO_TRY(advance_grid<Real>(blk_, advance_mode(cd_.pc.spec), nitems_, num_sms_, &blocks, &smem));
     cudaGraph_t graph;
     CUDA_TRY(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
-    for (int l = 0; l < nlaunch; ++l)
+    // one DFT pass per group of stage_group launches (and after the last launch):
+    // it sums the group's steps in time order, as one pass per launch would
+    const int group = stage_group_for(blk_.T), S = cd_.pc.S, T = blk_.T;
+    for (int l = 0; l < nlaunch; ++l) {
+        const bool last_of_group = (l + 1) % group == 0 || l == nlaunch - 1;
+        const int n0 = (l - l % group) * T;
+        const int nlev = last_of_group ? std::min((l + 1) * T, S) - n0 : 0;
         launch_advance<Real>(blk_, advance_mode(cd_.pc.spec), blocks, smem, d_descs_.as<SolveDesc<Real>>(),
                              d_items_.as<WorkItem>(), nitems_, nsolves_, d_counter_.as<int>(), dft_contour(cd_.pc),
-                             stream_);
+                             stream_, n0, nlev);
+    }
     cudaError_t ce = cudaStreamEndCapture(stream_, &graph);
     if (ce != cudaSuccess) return fail(TOMO_ECUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
     ce = cudaGraphInstantiate(&graph_exec_, graph, 0);
@@ -719,6 +726,8 @@ int EngineT<Real>::forward(const double* args, size_t ncand, size_t nparam, cons
     h_descs_.resize(nsolves);
     fill_descs<Real>(cd_, up_, d_state_.as<Real>(), d_mats_.as<uint8_t>(), d_tabs_.as<Real>(), h_descs_.data());
     if (pc.extra) h_descs_[nsolves - 1] = incident_desc<Real>(cd_, d_state_.as<Real>() + (size_t)(nsolves - 1) * cd_.lay.per_solve);
+    if (!s.plain)   // the time-loop graph runs one DFT pass per group of launches
+        for (SolveDesc<Real>& D : h_descs_) D.stage_group = stage_group_for(blk_.T);
     CUDA_TRY(cudaMemcpyAsync(d_descs_.p, h_descs_.data(), sizeof(SolveDesc<Real>) * nsolves, cudaMemcpyHostToDevice,
                              stream_));
     h2d += sizeof(SolveDesc<Real>) * nsolves;
@@ -742,7 +751,8 @@ int EngineT<Real>::forward(const double* args, size_t ncand, size_t nparam, cons
         CUDA_TRY(cudaEventRecord(ev_[1], stream_));
         CUDA_TRY(cudaGraphLaunch(graph_exec_, stream_));
         CUDA_TRY(cudaEventRecord(ev_[2], stream_));
-        kernels += (dft_contour(pc) > 0 ? 3 : 2) * (int64_t)nlaunch;
+        const int group = stage_group_for(blk_.T);
+        kernels += 2 * (int64_t)nlaunch + (dft_contour(pc) > 0 ? (nlaunch + group - 1) / group : 0);
     }
 
     CUDA_TRY(cudaMemsetAsync(d_flag_.p, 0, sizeof(int) * 4, stream_));

@@ -234,7 +234,7 @@ void fill_descs(const ClassData<Real>& cd, const Unpacked& u, Real* state_base, 
         SolveDesc<Real> D{};
         Real* sb = state_base + (size_t)sv * L.per_solve;
         D.nx = s.nx; D.ny = s.ny; D.pitch = pc.pitch; D.mpitch = pc.mpitch;
-        D.ncpml = pc.nc; D.steps_total = pc.S; D.step = 0; D.parity = 0; D.active = 1; D.nmat = pc.nmat;
+        D.ncpml = pc.nc; D.steps_total = pc.S; D.step = 0; D.parity = 0; D.active = 1; D.nmat = pc.nmat; D.stage_group = 1;
         D.nrx = pc.nrx; D.nf_d = s.nf2ff_d; D.nfreq = pc.nfreq; D.n_contour = pc.C;
         D.chez = (Real)pc.chez; D.Kp = (Real)pc.Kp; D.dx = (Real)s.dx;
         Real* f = sb + kPadLeft;
@@ -292,7 +292,7 @@ SolveDesc<Real> incident_desc(const ClassData<Real>& cd, Real* state) {
     const SolveLayout& L = cd.lay;
     SolveDesc<Real> D{};
     D.nx = s.nx; D.ny = s.ny; D.pitch = pc.pitch; D.mpitch = pc.mpitch;
-    D.ncpml = pc.nc; D.steps_total = pc.S; D.step = 0; D.parity = 0; D.active = 1; D.nmat = 1;
+    D.ncpml = pc.nc; D.steps_total = pc.S; D.step = 0; D.parity = 0; D.active = 1; D.nmat = 1; D.stage_group = 1;
     D.nrx = 0; D.nf_d = s.nf2ff_d; D.nfreq = pc.nfreq; D.n_contour = pc.C;
     D.chez = (Real)pc.chez; D.Kp = (Real)pc.Kp; D.dx = (Real)s.dx;
     Real* f = state + kPadLeft;
@@ -405,19 +405,27 @@ std::vector<Blocking> tune_candidates(int mode, int fixT, int fixCols, int fixMi
 template <typename Real>
 int launch_plain_step(int mode, const SolveDesc<Real>* d, int n, int nx, int ny, int n_contour, cudaStream_t st);
 
-// One advance launch (T steps of every listed solve), then the running DFT of
-// the contours staged by it (when cmax, the largest contour among the solves,
-// is positive), then the progress bump.  Returns the number of kernels.
+// Launches whose contour samples one DFT pass sums (the stage_group of the
+// engine's descriptors at blocking T).
+inline int stage_group_for(int T) { return std::max(1, kStageLevels / std::max(T, 1)); }
+
+// One advance launch (T steps of every listed solve), then -- when cmax, the
+// largest contour among the solves, is positive and dft_nlev is not 0 -- the
+// running DFT of the staged contour samples (dft_n0 < 0: this launch's levels;
+// else steps dft_n0 .. dft_n0 + dft_nlev - 1), then the progress bump.
+// Returns the number of kernels.
 template <typename Real>
 int launch_advance(const Blocking& b, int mode, int blocks, size_t smem, const SolveDesc<Real>* descs,
-                   const WorkItem* items, int nitems, int nsolves, int* counter, int cmax, cudaStream_t st) {
+                   const WorkItem* items, int nitems, int nsolves, int* counter, int cmax, cudaStream_t st,
+                   int dft_n0 = -1, int dft_nlev = -1) {
     AdvanceFn<Real> fn = advance_kernel_for<Real>(b, mode);
     fn<<<blocks, 128, smem, st>>>(descs, items, nitems, counter);
-    if (cmax > 0)
-        dft_accumulate_kernel<Real><<<dim3(nsolves, (cmax + 127) / 128), 128, 0, st>>>(descs, b.T);
+    const bool dft = cmax > 0 && dft_nlev != 0;
+    if (dft)
+        dft_accumulate_kernel<Real><<<dim3(nsolves, (cmax + 127) / 128), 128, 0, st>>>(descs, b.T, dft_n0, dft_nlev);
     bump_kernel<Real><<<(nsolves + 127) / 128, 128, 0, st>>>(const_cast<SolveDesc<Real>*>(descs), nsolves, b.T,
                                                             counter);
-    return cmax > 0 ? 3 : 2;
+    return dft ? 3 : 2;
 }
 
 // Largest NTFF contour of a class as launch_advance wants it (0: no NTFF).

@@ -199,13 +199,23 @@ struct Vec4<double> {
     }
 };
 
+// The staging buffer holds kStageLevels levels: a launch of T steps writes its
+// levels at slot ((step / T) % stage_group) * T, so stage_group launches fill
+// it before one pass of this kernel sums them.  Called with n0 >= 0 (steps
+// n0 .. n0 + nlev - 1 in slots 0 .. nlev - 1, the engine's fixed time loop) or
+// with n0 < 0 (the levels of the launch that starts at the solve's current
+// step, stage_group = 1: the serving loop, whose solves differ in progress).
+constexpr int kStageLevels = 8;
+
 template <typename Real>
-__global__ void __launch_bounds__(128) dft_accumulate_kernel(const SolveDesc<Real>* __restrict__ descs, int T) {
+__global__ void __launch_bounds__(128) dft_accumulate_kernel(const SolveDesc<Real>* __restrict__ descs, int T,
+                                                             int n0_group, int nlev) {
     const SolveDesc<Real>& D = descs[blockIdx.x];
     const int c = blockIdx.y * blockDim.x + threadIdx.x;
     const int C = D.n_contour, nfreq = D.nfreq;
     if (!D.active || nfreq <= 0 || c >= C) return;
-    const int n0 = D.step, nsteps = min(T, D.steps_total - n0);
+    const int n0 = n0_group >= 0 ? n0_group : D.step;
+    const int nsteps = min(n0_group >= 0 ? nlev : T, D.steps_total - n0);
     for (int f = 0; f < nfreq; ++f) {
         Real* a = D.acc + ((size_t)f * C + c) * 8;
         Real j[4], mm[4];   // J: sum re, sum im, comp re, comp im; M likewise
@@ -318,7 +328,8 @@ __device__ void advance_item(const SolveDesc<Real>* __restrict__ Dp, const WorkI
     const int psy_h = psy0, psy_e = psy0 + 2 * nc * (nx + 1);         // y-strip psi sub-arrays
     const uint8_t* __restrict__ matp = D.mat;
     Real* const cpml = ws.cpml;   // CPML profile, copied to shared memory below
-    Real* __restrict__ stage = D.stage;   // [T][C][2] contour samples of this launch's levels
+    // [T][C][2] contour samples of this launch's levels, in its slots of the staging buffer
+    Real* __restrict__ stage = D.stage + (size_t)((n0 / T) % D.stage_group) * T * C * 2;
     const int mpitch = D.mpitch, jx0 = D.jx0, jx1 = D.jx1, jy0 = D.jy0, jy1 = D.jy1;
     const int src_x = D.src_x, src_y = D.src_y;
 

@@ -52,6 +52,7 @@ struct SolveDesc {
     int psi_stride;              // elements per psi time copy
     int active;                  // 0: skip this solve
     int nmat;                    // materials in use: indices 0 .. nmat-1 of mtab
+    int stage_group;             // launches that fill the contour staging buffer before one DFT pass
     Real chez;                   // dt/(mu0 dx)
     Real Kp;                     // Debye recursion coefficient
     Real dx;
@@ -72,8 +73,8 @@ struct SolveDesc {
     Real* traces;                // [nrx][steps_total]
     const Real* phasor;          // [steps_total][nfreq][4]: dt*exp(-jwn dt), dt*exp(-jw(n+1/2)dt)
     Real* acc;                   // [nfreq][n_contour][8]: J sum re/im, J comp re/im, M sum, M comp
-    Real* stage;                 // [T][n_contour][2]: (h, e) contour samples of the levels of the last
-                                 // advance launch, summed into acc by the DFT kernel
+    Real* stage;                 // [8][n_contour][2]: (h, e) contour samples of the levels of the last
+                                 // stage_group advance launches, summed into acc by the DFT kernel
     // plane wave (reference modes): g = exp(-(ar/tau)^2),
     // ar = (t dt - t0 + l/c0) - (ky (y - yoff) + kx (x - xoff)) dx/c0
     double pw_kx, pw_ky, pw_xoff, pw_yoff, pw_t0l, pw_inv_tau, pw_dxc0, dt;
