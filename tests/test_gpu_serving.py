@@ -178,3 +178,21 @@ def test_bounded_wait(tomo):
         assert s.poll(t, 2) is None          # still queued
         got = s.wait(t, 2, 120.0)
         np.testing.assert_array_equal(got, batch)
+
+
+def test_reference_mode_request_equals_batch(tomo):
+    """A request in the reference GPU mode (plane waves, far-field misfit, the
+    far field computed on the device for the misfit) gives the batch path's
+    fitness bit for bit."""
+    from tomography_gb300 import workloads as W
+
+    spec = tomo.reference_spec(False).copy(steps=300)
+    args = np.stack([W.reference_patch_args(900 + k) for k in range(2)])
+    with tomo.Solver(spec) as s:
+        target = s.forward(W.reference_patch_args(950), traces=False, far_field=True)["D"][0]
+        s.set_target(target.ravel())
+        batch = s.fitness_batch(args)
+        t = s.submit(args)
+        got = s.wait(t, 2, 120.0)
+    np.testing.assert_array_equal(got, batch)
+    assert np.all(batch < 0)
