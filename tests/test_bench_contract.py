@@ -60,3 +60,17 @@ def test_both_arms_report_the_same_config():
     out = _run({})
     d = json.loads([l for l in out.stdout.splitlines() if l.strip()][0])
     assert d["config"] == bench.workload_config(1, bench.N_CAND)
+
+
+def test_profile_summary_covers_the_autotuned_blockings():
+    """The roofline's DRAM traffic comes from the committed ncu summary; it holds
+    a capture (with its per-cell-update DRAM bytes) for each blocking the
+    autotuner picks between on the PSO generation, and none for others."""
+    import bench
+
+    t4 = bench._profile_traffic(4, 2, 2)
+    t2 = bench._profile_traffic(2, 2, 3)
+    assert t4 is not None and t2 is not None
+    # deeper temporal blocking moves fewer DRAM bytes per cell-update, both far below 48 B
+    assert 0 < t4 < t2 < bench.BYTES_PER_CELL_UPDATE
+    assert bench._profile_traffic(3, 1, 3) is None
