@@ -4,10 +4,14 @@ Python mirror of the reference's operator interface.  The reference exposes
 ``double FDTD_GPU(const std::vector<double>&)`` (FDTD_GPU.cuh:8) and tao's
 search drivers call it once per candidate (test.cxx:94-121).  Here the same
 entry point is :func:`FDTD_GPU`, and the batched / serving interfaces of the
-native library are exposed through :class:`Solver`.  Everything runs in the
-native library ``_lib/libtomography_gb300.so`` (hand-written sm_103a CUDA
-kernels behind the C ABI of ``include/tomography.h``); there is no Python or
-CPU fallback: if the library cannot be loaded, every call raises.
+native library are exposed through :class:`Solver` (``forward``,
+``fitness_batch``, ``submit`` / ``serve_step`` / ``poll`` / ``wait``).  The
+search drivers that stand in for tao's are in :mod:`tomography_gb300.search`;
+the legacy total-field far field is ``reference_spec().copy(total_field=1)``.
+Everything runs in the native library ``_lib/libtomography_gb300.so``
+(hand-written sm_103a CUDA kernels behind the C ABI of
+``include/tomography.h``); there is no Python or CPU fallback: if the library
+cannot be loaded, every call raises.
 """
 from __future__ import annotations
 
