@@ -1,0 +1,32 @@
+"""Analytic known answers on the GPU.
+
+Mirror symmetry: the Yee grid with its CPML is symmetric under y -> ny - y, so
+with the transmitter on the symmetry row and a phantom symmetric about it, the
+receivers k and N - k record the same trace.  Mirrored cells evaluate the same
+explicitly rounded operations on the same values, so the traces are equal bit
+for bit, in FP32 and FP64, at every blocking; and they match the FP64 oracle
+(traces rel-L2 <= 1e-5 in FP32, <= 1e-10 in FP64).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from helpers import rel_l2
+from test_oracle import MIRROR_PARAMS, _mirror_spec
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("blocking", [(0, 0), (4, 2), (2, 1)])
+def test_mirror_symmetry(tomo, oracle, blocking):
+    T, cols = blocking
+    spec = _mirror_spec(tomo)
+    ref = oracle.breast_forward(spec.as_dict(), MIRROR_PARAMS, bits=64)["traces"][0]
+    for prec, tol in ((tomo.FP32, 1e-5), (tomo.FP64, 1e-10)):
+        c = cols if prec == tomo.FP32 else min(cols, 1)
+        with tomo.Solver(spec.copy(precision=prec, steps_per_launch=T, cols_per_lane=c)) as s:
+            tr = s.forward(MIRROR_PARAMS, traces=True, traces_f64=True, far_field=False)["traces_f64"][0][0]
+        for k in range(1, 8):
+            np.testing.assert_array_equal(tr[k], tr[16 - k])
+        assert rel_l2(tr, ref) <= tol, prec
