@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 from helpers import rel_l2
-from test_oracle import MIRROR_PARAMS, _mirror_spec
+from test_oracle import MIRROR_PARAMS, _mirror_spec, assert_doubled
 
 pytestmark = pytest.mark.gpu
 
@@ -30,3 +30,17 @@ def test_mirror_symmetry(tomo, oracle, blocking):
         for k in range(1, 8):
             np.testing.assert_array_equal(tr[k], tr[16 - k])
         assert rel_l2(tr, ref) <= tol, prec
+
+
+def test_source_linearity_exact(tomo):
+    """Twice the source amplitude gives exactly twice every trace: in FP64
+    everywhere, in FP32 wherever |2a| >= 1e-30 (the arrival's leading edge
+    passes through subnormal values, where doubling and rounding do not
+    commute; those differences stay below 1.2e-38)."""
+    spec = _mirror_spec(tomo)
+    for prec in (tomo.FP32, tomo.FP64):
+        out = {}
+        for amp in (1.0e3, 2.0e3):
+            with tomo.Solver(spec.copy(precision=prec, src_amp=amp)) as s:
+                out[amp] = s.forward(MIRROR_PARAMS, traces=True, traces_f64=True, far_field=False)["traces_f64"][0]
+        assert_doubled(out[2.0e3], out[1.0e3], 64 if prec == tomo.FP64 else 32)

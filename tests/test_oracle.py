@@ -359,6 +359,22 @@ def _mirror_spec(tomo):
 MIRROR_PARAMS = np.array([0.0, 0.0, 8e-3, 8e-3, 0.0, 30.0, 15.0, 0.4])
 
 
+def assert_doubled(b, a, bits):
+    """b == 2 a exactly in FP64.  In FP32 the leading edge of an arrival passes
+    through subnormal values (below 1.2e-38), which carry fewer bits, so there
+    doubling and rounding do not commute; the differences stay at that scale
+    (|b - 2a| <= 1.2e-38 everywhere) and b == 2 a exactly wherever |2a| >= 1e-30."""
+    b, a = np.asarray(b, dtype=np.float64), np.asarray(a, dtype=np.float64)
+    if bits == 64:
+        np.testing.assert_array_equal(b, 2.0 * a)
+        return
+    tiny = np.finfo(np.float32).tiny
+    assert np.all(np.abs(b - 2.0 * a) <= tiny)
+    big = np.abs(2.0 * a) >= 1e-30
+    np.testing.assert_array_equal(b[big], 2.0 * a[big])
+    assert big.mean() > 0.5   # most samples follow the arrival
+
+
 def test_oracle_mirror_symmetry(tomo, oracle):
     """The Yee grid with its CPML is symmetric under y -> ny - y (Hx changes
     sign), so with the source on the symmetry row the receivers k and 16 - k
@@ -374,3 +390,14 @@ def test_oracle_mirror_symmetry(tomo, oracle):
         for k in range(1, 8):
             np.testing.assert_array_equal(tr[k], tr[16 - k])
         assert np.abs(tr[1]).max() > 1e-3
+
+
+def test_oracle_source_linearity_exact(tomo, oracle):
+    """The solve is linear in the source and doubling is exact in floating
+    point, so twice the source amplitude gives twice every trace (exactly in
+    FP64; in FP32 up to subnormal-scale differences, see assert_doubled)."""
+    spec = _mirror_spec(tomo).as_dict()
+    for bits in (64, 32):
+        a = oracle.breast_forward(dict(spec, src_amp=1.0e3), MIRROR_PARAMS, bits=bits)["traces"]
+        b = oracle.breast_forward(dict(spec, src_amp=2.0e3), MIRROR_PARAMS, bits=bits)["traces"]
+        assert_doubled(b, a, bits)
