@@ -44,3 +44,20 @@ def test_source_linearity_exact(tomo):
             with tomo.Solver(spec.copy(precision=prec, src_amp=amp)) as s:
                 out[amp] = s.forward(MIRROR_PARAMS, traces=True, traces_f64=True, far_field=False)["traces_f64"][0]
         assert_doubled(out[2.0e3], out[1.0e3], 64 if prec == tomo.FP64 else 32)
+
+
+def test_reciprocity(tomo):
+    """The GPU solves keep the scheme's reciprocity: trace(tx a, rx b) equals
+    trace(tx b, rx a) for every antenna pair, to rel-L2 <= 1e-12 in FP64 and
+    <= 1e-5 in FP32."""
+    from tomography_gb300 import workloads as W
+
+    from helpers import small_params
+    from test_oracle import _reciprocity_spec, reciprocity_error
+
+    spec = _reciprocity_spec(tomo)
+    params = small_params(W, 3)
+    for prec, tol in ((tomo.FP64, 1e-12), (tomo.FP32, 1e-5)):
+        with tomo.Solver(spec.copy(precision=prec)) as s:
+            tr = s.forward(params, traces=True, traces_f64=True, far_field=False)["traces_f64"][0]
+        assert reciprocity_error(tr) <= tol, prec

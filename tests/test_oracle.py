@@ -401,3 +401,31 @@ def test_oracle_source_linearity_exact(tomo, oracle):
         a = oracle.breast_forward(dict(spec, src_amp=1.0e3), MIRROR_PARAMS, bits=bits)["traces"]
         b = oracle.breast_forward(dict(spec, src_amp=2.0e3), MIRROR_PARAMS, bits=bits)["traces"]
         assert_doubled(b, a, bits)
+
+
+def _reciprocity_spec(tomo):
+    from helpers import small_breast_spec
+
+    return small_breast_spec(tomo, n_antennas=8, n_tx=8, steps=500)
+
+
+def reciprocity_error(traces) -> float:
+    """max over antenna pairs of rel-L2(trace(tx a, rx b), trace(tx b, rx a))."""
+    n = traces.shape[0]
+    return max(np.linalg.norm(traces[a][b] - traces[b][a]) / np.linalg.norm(traces[a][b])
+               for a in range(n) for b in range(a + 1, n))
+
+
+def test_oracle_reciprocity(tomo, oracle):
+    """Reciprocity of the discrete scheme: with every antenna in the same
+    background material, the trace of transmitter a at receiver b equals the
+    trace of b at a, through a heterogeneous Debye phantom and the CPML --
+    to rounding (measured: 6e-16 in FP64, 4e-7 in FP32)."""
+    from tomography_gb300 import workloads as W
+
+    from helpers import small_params
+
+    spec = _reciprocity_spec(tomo).as_dict()
+    params = small_params(W, 3)
+    assert reciprocity_error(oracle.breast_forward(spec, params, bits=64)["traces"]) <= 1e-13
+    assert reciprocity_error(oracle.breast_forward(spec, params, bits=32)["traces"]) <= 1e-5
