@@ -229,15 +229,17 @@ int tomo_get_stats(tomo_handle *h, tomo_stats *stats);
    first batch. */
 int tomo_field_snapshot(tomo_handle *h, size_t candidate, int excitation, int field, float *out, size_t n);
 
-/* ---- search drivers: synchronous particle swarm and differential evolution
-   over whole generations, the drop-in for tao's ParticleSwarmMPI /
-   DifferentialEvolutionMPI in the reference's driver (test.cxx:82-121,
-   `ps(min_bound, max_bound, arguments); ps.go(FDTD_GPU)`).  One call of the
-   batch fitness function evaluates a whole generation; fitness is maximised.
-   Host code only: runs without a GPU when the fitness function needs none. */
-enum { TOMO_SEARCH_PS = 0, TOMO_SEARCH_DE = 1 };
+/* ---- search drivers: synchronous particle swarm, differential evolution and
+   a regression Newton method over whole generations, the drop-in for tao's
+   ParticleSwarmMPI / DifferentialEvolutionMPI / AsynchronousNewtonMethod in
+   the reference's driver (test.cxx:82-121, `ps(min_bound, max_bound,
+   arguments); ps.go(FDTD_GPU)`, `anm(min_bound, max_bound, radius, arguments);
+   anm.iterate(FDTD_GPU)`).  One call of the batch fitness function evaluates
+   a whole generation; fitness is maximised.  Host code only: runs without a
+   GPU when the fitness function needs none. */
+enum { TOMO_SEARCH_PS = 0, TOMO_SEARCH_DE = 1, TOMO_SEARCH_ANM = 2 };
 typedef struct tomo_search_params {
-    int32_t type;                 /* TOMO_SEARCH_PS or TOMO_SEARCH_DE                   */
+    int32_t type;                 /* TOMO_SEARCH_PS, TOMO_SEARCH_DE or TOMO_SEARCH_ANM  */
     int32_t population_size;      /* --population_size (>= 4)                            */
     int32_t maximum_iterations;   /* --maximum_iterations (generations after the first)  */
     int32_t number_pairs;         /* DE --number_pairs: difference vectors per donor     */
@@ -249,6 +251,20 @@ typedef struct tomo_search_params {
     double differential_scale;    /* DE --differential_scale                             */
     int32_t parent_best;          /* DE --parent_selection: 1 best, 0 random             */
     int32_t reserved;
+    /* Newton method: each iteration samples regression_size points within
+       radius of the best point so far (one batch), fits a quadratic model by
+       least squares, and evaluates line_search_size points c + a s along the
+       Newton step s, a from line_search_min to line_search_max (one batch).   */
+    const double *radius;         /* ANM per-parameter sampling radius (n_param values);
+                                     NULL: a tenth of max_bound - min_bound           */
+    int32_t regression_size;      /* ANM --regression_size; 0: twice the model's unknowns */
+    int32_t line_search_size;     /* ANM --line_search_size (>= 2)                       */
+    double line_search_min;       /* ANM --line_search_min                               */
+    double line_search_max;       /* ANM --line_search_max                               */
+    int32_t hessian_diagonal;     /* ANM --hessian_diagonal 1: fit only the Hessian's
+                                     diagonal (1 + 2k unknowns instead of
+                                     1 + k + k(k+1)/2 for k free parameters)          */
+    int32_t reserved2;
 } tomo_search_params;
 /* fitness[i] of population[i*n_param ...], i < n_cand; non-zero return aborts the search */
 typedef int (*tomo_batch_fitness_fn)(void *user, const double *population, size_t n_cand, size_t n_param,
@@ -259,8 +275,9 @@ int tomo_search_defaults(tomo_search_params *p, int type);
 /* tao-style "--name value" arguments over the defaults; unknown names are skipped */
 int tomo_search_parse_args(tomo_search_params *p, int argc, const char *const *argv);
 /* best_params: n_param doubles; history (may be NULL): maximum_iterations + 1
-   best fitness values, the first after the initial generation; evaluations
-   (may be NULL): candidates evaluated */
+   best fitness values, the first after the initial generation (the Newton
+   method: its starting point, the bounds' midpoint); evaluations (may be
+   NULL): candidates evaluated */
 int tomo_search_run(const tomo_search_params *p, const double *min_bound, const double *max_bound, size_t n_param,
                     tomo_batch_fitness_fn f, void *user, tomo_generation_fn report, void *report_user,
                     double *best_params, double *best_fitness, double *history, int64_t *evaluations);

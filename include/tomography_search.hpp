@@ -8,6 +8,7 @@
 //
 //   tomo::ParticleSwarm ps(min_bound, max_bound, arguments);  ps.go(FDTD_GPU);
 //   tomo::DifferentialEvolution de(min_bound, max_bound, arguments);  de.go(batch_fitness);
+//   tomo::NewtonMethod anm(min_bound, max_bound, radius, arguments);  anm.iterate(FDTD_GPU);
 //
 // go() takes either the reference's per-candidate fitness type
 // (double (*)(const std::vector<double>&), one call per candidate) or a batch
@@ -18,7 +19,9 @@
 // tao's "--name value" pairs: --population_size, --maximum_iterations, --seed,
 // --inertia, --local_best_weight, --global_best_weight (particle swarm),
 // --crossover_rate, --differential_scale, --number_pairs, --parent_selection
-// best|random (differential evolution).  Errors throw std::runtime_error
+// best|random (differential evolution), --regression_size, --line_search_size,
+// --line_search_min, --line_search_max, --hessian_diagonal (Newton method).
+// Errors throw std::runtime_error
 // (std::invalid_argument for bad bounds or arguments).
 #ifndef TOMOGRAPHY_SEARCH_HPP
 #define TOMOGRAPHY_SEARCH_HPP
@@ -125,6 +128,34 @@ class DifferentialEvolution : public Search {
     DifferentialEvolution(const std::vector<double>& min_bound, const std::vector<double>& max_bound,
                           const std::vector<std::string>& arguments = {})
         : Search(TOMO_SEARCH_DE, min_bound, max_bound, arguments) {}
+};
+
+// Regression Newton method with the construction of tao's
+// AsynchronousNewtonMethod (min_bound, max_bound, radius, arguments) and its
+// iterate(f) (test.cxx:116-121).  Arguments: --maximum_iterations,
+// --regression_size, --line_search_size, --line_search_min,
+// --line_search_max, --hessian_diagonal, --seed.
+class NewtonMethod : public Search {
+   public:
+    NewtonMethod(const std::vector<double>& min_bound, const std::vector<double>& max_bound,
+                 const std::vector<double>& radius, const std::vector<std::string>& arguments = {})
+        : Search(TOMO_SEARCH_ANM, min_bound, max_bound, arguments), radius_(radius) {
+        if (radius_.size() != min_bound.size())
+            throw std::invalid_argument("radius must have one value per parameter");
+    }
+    SearchResult go(const BatchFitness& f, const std::function<void(int, double, const double*)>& report = {}) {
+        params().radius = radius_.data();
+        return Search::go(f, report);
+    }
+    SearchResult go(double (*f)(const std::vector<double>&)) {
+        params().radius = radius_.data();
+        return Search::go(f);
+    }
+    SearchResult iterate(const BatchFitness& f) { return go(f); }
+    SearchResult iterate(double (*f)(const std::vector<double>&)) { return go(f); }
+
+   private:
+    std::vector<double> radius_;
 };
 
 }  // namespace tomo

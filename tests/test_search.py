@@ -176,6 +176,8 @@ int main() {
     });
     tomo::DifferentialEvolution de(lo, hi, {"--population_size", "30", "--maximum_iterations", "150"});
     tomo::SearchResult b = de.go(sphere);
+    tomo::NewtonMethod anm(lo, hi, std::vector<double>(5, 1.0), {"--maximum_iterations", "2"});
+    tomo::SearchResult c = anm.iterate(sphere);
     bool threw = false;
     try {
         tomo::ParticleSwarm bad(hi, lo);
@@ -183,8 +185,8 @@ int main() {
     } catch (const std::exception&) {
         threw = true;
     }
-    std::printf("%d %lld %zu %.9g %.9g %d\n", calls, (long long)a.evaluations, a.history.size(), a.best_fitness,
-                b.best_fitness, threw ? 1 : 0);
+    std::printf("%d %lld %zu %.9g %.9g %d %.9g\n", calls, (long long)a.evaluations, a.history.size(), a.best_fitness,
+                b.best_fitness, threw ? 1 : 0, c.best_fitness);
     return 0;
 }
 """
@@ -192,8 +194,9 @@ int main() {
 
 def test_cpp_drivers_have_the_tao_call_shape(tomo, tmp_path):
     """A C++ caller constructs the drivers as tao's are constructed in
-    test.cxx:82-121 (bounds, argument strings) and calls go() with a batch
-    lambda or with a function of the reference's fitness type."""
+    test.cxx:82-121 (bounds, radius, argument strings) and calls go() /
+    iterate() with a batch lambda or with a function of the reference's
+    fitness type."""
     import os
     import shutil
     import subprocess
@@ -213,3 +216,61 @@ def test_cpp_drivers_have_the_tao_call_shape(tomo, tmp_path):
     assert calls == 121 and evals == 30 * 121 and nhist == 121
     assert float(out[3]) > -1e-3 and float(out[4]) > -1e-2
     assert out[5] == "1"   # min > max bounds rejected
+    assert float(out[6]) > -1e-9   # the Newton method solves the quadratic
+
+
+def test_newton_method_solves_a_quadratic_in_one_step():
+    """On a concave quadratic the regression model is exact, so the first
+    Newton step (line-search multiple 1) lands on the optimum."""
+    lo, hi = np.full(5, -5.0), np.full(5, 5.0)
+    t = np.array([1.0, -2.0, 0.5, 3.0, -1.5])
+    w = np.array([1.0, 2.0, 0.5, 3.0, 1.5])
+    calls = []
+
+    def f(x):
+        calls.append(x.shape[0])
+        return -np.sum(w * (x - t) ** 2, axis=1)
+
+    res = S.NewtonMethod(lo, hi, np.ones(5), line_search_size=4, line_search_min=-1.0, line_search_max=2.0,
+                         maximum_iterations=2, seed=1).iterate(f)
+    assert res.best_fitness > -1e-9
+    np.testing.assert_allclose(res.best_params, t, atol=1e-5)
+    # start point, then per iteration one regression batch and one line-search batch
+    nu = 1 + 5 + 15
+    assert calls == [1, 2 * nu, 4, 2 * nu, 4] and res.evaluations == sum(calls)
+    assert all(b >= a for a, b in zip(res.history, res.history[1:]))
+
+
+def test_newton_method_non_quadratic_fixed_and_diagonal():
+    """A quartic objective improves every iteration; a parameter with
+    min == max stays fixed (test.cxx:70-73, sigma); the diagonal-Hessian model
+    solves a separable quadratic."""
+    lo = np.array([-3.0, -3.0, 0.0, -3.0])
+    hi = np.array([3.0, 3.0, 0.0, 3.0])
+    t = np.array([1.2, -0.7, 0.0, 2.1])
+    seen = []
+
+    def quartic(x):
+        seen.append(x[:, 2].copy())
+        d = x - t
+        return -np.sum(d ** 4 + d ** 2, axis=1)
+
+    res = S.NewtonMethod(lo, hi, np.full(4, 0.5), maximum_iterations=8, seed=2).go(quartic)
+    assert np.all(np.concatenate(seen) == 0.0)
+    assert res.history[-1] > res.history[0] and res.best_fitness > -1e-3
+    sep = S.NewtonMethod(lo, hi, np.full(4, 1.0), hessian_diagonal=1, maximum_iterations=1,
+                         line_search_size=4).go(lambda x: -np.sum((x - t) ** 2, axis=1))
+    assert sep.best_fitness > -1e-9
+
+
+def test_newton_method_arguments_like_tao():
+    argv = ["--maximum_iterations", "3", "--regression_size", "40", "--line_search_size", "5",
+            "--line_search_min", "-0.5", "--line_search_max", "1.5", "--hessian_diagonal", "1"]
+    nm = S.NewtonMethod(np.zeros(3), np.ones(3), np.full(3, 0.1), argv)
+    assert (nm.maximum_iterations, nm.regression_size, nm.line_search_size) == (3, 40, 5)
+    assert (nm.line_search_min, nm.line_search_max, nm.hessian_diagonal) == (-0.5, 1.5, 1)
+    with pytest.raises(ValueError):
+        S.NewtonMethod(np.zeros(3), np.ones(3), np.ones(2))
+    bad = S.NewtonMethod(np.zeros(3), np.ones(3), np.ones(3), line_search_size=1)
+    with pytest.raises(Exception):
+        bad.go(lambda x: -np.sum(x * x, axis=1))

@@ -92,6 +92,9 @@ class SearchParams(C.Structure):
         ("inertia", C.c_double), ("local_best_weight", C.c_double), ("global_best_weight", C.c_double),
         ("crossover_rate", C.c_double), ("differential_scale", C.c_double),
         ("parent_best", C.c_int32), ("reserved", C.c_int32),
+        ("radius", C.POINTER(C.c_double)), ("regression_size", C.c_int32), ("line_search_size", C.c_int32),
+        ("line_search_min", C.c_double), ("line_search_max", C.c_double), ("hessian_diagonal", C.c_int32),
+        ("reserved2", C.c_int32),
     ]
 
 

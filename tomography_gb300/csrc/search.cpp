@@ -1,17 +1,22 @@
 // Synchronous search drivers over whole generations: global-best particle
-// swarm and differential evolution (DE/{best,random}/k/bin).
+// swarm, differential evolution (DE/{best,random}/k/bin) and a regression
+// Newton method.
 //
-// They take the place of tao's ParticleSwarmMPI / DifferentialEvolutionMPI in
-// the reference's driver (test.cxx:82-121: `ps(min_bound, max_bound,
-// arguments); ps.go(FDTD_GPU)`).  tao farms one candidate per MPI rank and
+// They take the place of tao's ParticleSwarmMPI / DifferentialEvolutionMPI /
+// AsynchronousNewtonMethod in the reference's driver (test.cxx:82-121:
+// `ps(min_bound, max_bound, arguments); ps.go(FDTD_GPU)`, `anm(min_bound,
+// max_bound, radius, arguments); anm.iterate(FDTD_GPU)`).  tao farms one candidate per MPI rank and
 // call; here a generation is ONE call of a batch fitness function, so every
 // candidate x excitation solve of the generation advances together on the GPU
 // (tomo_fitness_batch).  tao is an un-vendored submodule: the algorithms are
 // the textbook synchronous forms with tao's parameter names
 // (--population_size, --maximum_iterations, --inertia, --local_best_weight,
 // --global_best_weight, --crossover_rate, --differential_scale,
-// --number_pairs, --parent_selection, --seed).  Fitness is maximised (the
+// --number_pairs, --parent_selection, --seed; the Newton method's
+// --regression_size, --line_search_size, --line_search_min,
+// --line_search_max and --hessian_diagonal are this implementation's).  Fitness is maximised (the
 // reference's fitness is a negative misfit).
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdlib>
@@ -172,13 +177,143 @@ int differential_evolution(Run& R, Rng& g, double* best_params, double* best_fit
     return TOMO_OK;
 }
 
+// Solve A x = b (n x n, row-major, overwritten) by Gaussian elimination with
+// partial pivoting; false when A is singular to working precision.
+bool solve_dense(std::vector<double>& A, std::vector<double>& b, size_t n) {
+    double scale = 0;
+    for (double v : A) scale = std::max(scale, std::fabs(v));
+    if (!(scale > 0)) return false;
+    for (size_t c = 0; c < n; ++c) {
+        size_t piv = c;
+        for (size_t r = c + 1; r < n; ++r)
+            if (std::fabs(A[r * n + c]) > std::fabs(A[piv * n + c])) piv = r;
+        if (!(std::fabs(A[piv * n + c]) > 1e-13 * scale)) return false;
+        if (piv != c) {
+            for (size_t k = 0; k < n; ++k) std::swap(A[c * n + k], A[piv * n + k]);
+            std::swap(b[c], b[piv]);
+        }
+        for (size_t r = c + 1; r < n; ++r) {
+            const double f = A[r * n + c] / A[c * n + c];
+            if (f == 0) continue;
+            for (size_t k = c; k < n; ++k) A[r * n + k] -= f * A[c * n + k];
+            b[r] -= f * b[c];
+        }
+    }
+    for (size_t c = n; c-- > 0;) {
+        double v = b[c];
+        for (size_t k = c + 1; k < n; ++k) v -= A[c * n + k] * b[k];
+        b[c] = v / A[c * n + c];
+    }
+    return true;
+}
+
+// Regression Newton method (the synchronous form of a Newton search driven by
+// sampled fitness values).  The free parameters are those with max > min; the
+// model is in scaled offsets z = (x - c) / radius from the best point c:
+//   f ~ b0 + g.z + sum_a h_aa z_a^2 / 2 + sum_{a<b} h_ab z_a z_b   (full)
+//   f ~ b0 + g.z + sum_a h_aa z_a^2 / 2                           (diagonal),
+// fitted by least squares (normal equations with a small ridge).  The Newton
+// step solves H s = -g (gradient step if H is singular); the line search
+// evaluates c + a s for a evenly spaced in [line_search_min, line_search_max]
+// (both directions, so a saddle of the model is not followed blindly).  The
+// best point seen becomes the next centre.
+int newton_method(Run& R, Rng& g, double* best_params, double* best_fitness, double* history) {
+    const size_t P = R.np;
+    std::vector<size_t> act;
+    for (size_t j = 0; j < P; ++j)
+        if (R.hi[j] > R.lo[j]) act.push_back(j);
+    const size_t k = act.size();
+    const bool diag = R.p.hessian_diagonal != 0;
+    const size_t nq = diag ? k : k * (k + 1) / 2, nu = 1 + k + nq;
+    const size_t m = R.p.regression_size > 0 ? (size_t)R.p.regression_size : std::max<size_t>(2 * nu, nu + 4);
+    const size_t L = (size_t)R.p.line_search_size;
+    std::vector<double> rad(P);
+    for (size_t j = 0; j < P; ++j) rad[j] = R.p.radius ? std::fabs(R.p.radius[j]) : 0.1 * (R.hi[j] - R.lo[j]);
+    for (size_t a = 0; a < k; ++a)
+        if (!(rad[act[a]] > 0)) return fail(TOMO_EINVAL, "radius must be positive for every free parameter");
+    // start: the midpoint of the bounds
+    std::vector<double> c(P), fx;
+    for (size_t j = 0; j < P; ++j) c[j] = 0.5 * (R.lo[j] + R.hi[j]);
+    if (int rc = R.evaluate(c, 1, fx)) return rc;
+    double fc = fx[0];
+    if (history) history[0] = fc;
+    std::vector<double> X(m * P), Y(L * P), z(k), phi(nu), A(nu * nu), rhs(nu), H(k * k), step(k);
+    for (int it = 0; it < R.p.maximum_iterations; ++it) {
+        // 1. regression sample around c
+        for (size_t i = 0; i < m; ++i)
+            for (size_t j = 0; j < P; ++j)
+                X[i * P + j] = R.clip(j, c[j] + (R.hi[j] > R.lo[j] ? rad[j] * (2.0 * g.uniform() - 1.0) : 0.0));
+        if (int rc = R.evaluate(X, m, fx)) return rc;
+        // 2. least-squares quadratic model in z
+        std::fill(A.begin(), A.end(), 0.0);
+        std::fill(rhs.begin(), rhs.end(), 0.0);
+        for (size_t i = 0; i < m; ++i) {
+            if (!std::isfinite(fx[i])) continue;
+            for (size_t a = 0; a < k; ++a) z[a] = (X[i * P + act[a]] - c[act[a]]) / rad[act[a]];
+            size_t q = 0;
+            phi[q++] = 1.0;
+            for (size_t a = 0; a < k; ++a) phi[q++] = z[a];
+            for (size_t a = 0; a < k; ++a) {
+                if (diag) phi[q++] = 0.5 * z[a] * z[a];
+                else
+                    for (size_t b = a; b < k; ++b) phi[q++] = (a == b ? 0.5 : 1.0) * z[a] * z[b];
+            }
+            for (size_t u = 0; u < nu; ++u) {
+                rhs[u] += phi[u] * fx[i];
+                for (size_t v = 0; v < nu; ++v) A[u * nu + v] += phi[u] * phi[v];
+            }
+        }
+        double tr = 0;
+        for (size_t u = 0; u < nu; ++u) tr += A[u * nu + u];
+        for (size_t u = 0; u < nu; ++u) A[u * nu + u] += 1e-12 * tr / (double)nu;
+        bool have = k > 0 && solve_dense(A, rhs, nu);
+        // 3. Newton step (gradient step when the model's Hessian is singular)
+        if (have) {
+            std::fill(H.begin(), H.end(), 0.0);
+            size_t q = 1 + k;
+            for (size_t a = 0; a < k; ++a) {
+                if (diag) H[a * k + a] = rhs[q++];
+                else
+                    for (size_t b = a; b < k; ++b) H[a * k + b] = H[b * k + a] = rhs[q++];
+            }
+            for (size_t a = 0; a < k; ++a) step[a] = -rhs[1 + a];
+            std::vector<double> Hc = H;
+            if (!solve_dense(Hc, step, k))
+                for (size_t a = 0; a < k; ++a) step[a] = rhs[1 + a];
+        }
+        // 4. line search along the step (in parameter units)
+        if (have)
+            for (size_t l = 0; l < L; ++l) {
+                const double al = R.p.line_search_min +
+                                  (R.p.line_search_max - R.p.line_search_min) * (double)l / (double)(L - 1);
+                for (size_t j = 0; j < P; ++j) Y[l * P + j] = c[j];
+                for (size_t a = 0; a < k; ++a)
+                    Y[l * P + act[a]] = R.clip(act[a], c[act[a]] + al * step[a] * rad[act[a]]);
+            }
+        std::vector<double> fy;
+        if (have)
+            if (int rc = R.evaluate(Y, L, fy)) return rc;
+        // 5. the best point seen becomes the centre
+        for (size_t i = 0; i < m; ++i)
+            if (fx[i] > fc) { fc = fx[i]; std::memcpy(c.data(), &X[i * P], sizeof(double) * P); }
+        for (size_t l = 0; l < fy.size(); ++l)
+            if (fy[l] > fc) { fc = fy[l]; std::memcpy(c.data(), &Y[l * P], sizeof(double) * P); }
+        if (history) history[it + 1] = fc;
+        if (R.report) R.report(R.report_user, it, fc, c.data());
+    }
+    std::memcpy(best_params, c.data(), sizeof(double) * P);
+    *best_fitness = fc;
+    return TOMO_OK;
+}
+
 }  // namespace
 
 extern "C" {
 
 int tomo_search_defaults(tomo_search_params* p, int type) {
     if (!p) return fail(TOMO_EINVAL, "tomo_search_defaults: NULL params");
-    if (type != TOMO_SEARCH_PS && type != TOMO_SEARCH_DE) return fail(TOMO_EINVAL, "unknown search type");
+    if (type != TOMO_SEARCH_PS && type != TOMO_SEARCH_DE && type != TOMO_SEARCH_ANM)
+        return fail(TOMO_EINVAL, "unknown search type");
     std::memset(p, 0, sizeof(*p));
     p->type = type;
     p->population_size = 50;
@@ -191,6 +326,13 @@ int tomo_search_defaults(tomo_search_params* p, int type) {
     p->differential_scale = 0.5;
     p->number_pairs = 1;
     p->parent_best = 1;
+    p->radius = nullptr;
+    p->regression_size = 0;
+    p->line_search_size = 13;   // a step of 0.25 over [-1, 2]: the full Newton step a = 1 is one of them
+    p->line_search_min = -1.0;
+    p->line_search_max = 2.0;
+    p->hessian_diagonal = 0;
+    if (type == TOMO_SEARCH_ANM) p->maximum_iterations = 10;
     return TOMO_OK;
 }
 
@@ -210,6 +352,11 @@ int tomo_search_parse_args(tomo_search_params* p, int argc, const char* const* a
         else if (a == "--crossover_rate") p->crossover_rate = std::strtod(v, &end);
         else if (a == "--differential_scale") p->differential_scale = std::strtod(v, &end);
         else if (a == "--number_pairs") p->number_pairs = (int32_t)std::strtol(v, &end, 10);
+        else if (a == "--regression_size") p->regression_size = (int32_t)std::strtol(v, &end, 10);
+        else if (a == "--line_search_size") p->line_search_size = (int32_t)std::strtol(v, &end, 10);
+        else if (a == "--line_search_min") p->line_search_min = std::strtod(v, &end);
+        else if (a == "--line_search_max") p->line_search_max = std::strtod(v, &end);
+        else if (a == "--hessian_diagonal") p->hessian_diagonal = (int32_t)std::strtol(v, &end, 10);
         else if (a == "--parent_selection") {
             const std::string s = v;
             if (s != "best" && s != "random") return fail(TOMO_EINVAL, "--parent_selection must be best or random");
@@ -226,19 +373,25 @@ int tomo_search_run(const tomo_search_params* p, const double* min_bound, const 
                     double* best_params, double* best_fitness, double* history, int64_t* evaluations) {
     if (!p || !min_bound || !max_bound || !f || !best_params || !best_fitness)
         return fail(TOMO_EINVAL, "tomo_search_run: NULL argument");
-    if (p->type != TOMO_SEARCH_PS && p->type != TOMO_SEARCH_DE) return fail(TOMO_EINVAL, "unknown search type");
+    if (p->type != TOMO_SEARCH_PS && p->type != TOMO_SEARCH_DE && p->type != TOMO_SEARCH_ANM)
+        return fail(TOMO_EINVAL, "unknown search type");
     if (n_param < 1) return fail(TOMO_EINVAL, "no parameters");
     for (size_t j = 0; j < n_param; ++j)
         if (!std::isfinite(min_bound[j]) || !std::isfinite(max_bound[j]) || max_bound[j] < min_bound[j])
             return fail(TOMO_EINVAL, "bounds must be finite with min <= max");
-    if (p->population_size < 4) return fail(TOMO_EINVAL, "population_size must be at least 4");
+    if (p->type != TOMO_SEARCH_ANM && p->population_size < 4)
+        return fail(TOMO_EINVAL, "population_size must be at least 4");
+    if (p->type == TOMO_SEARCH_ANM &&
+        (p->line_search_size < 2 || p->regression_size < 0 || !(p->line_search_max > p->line_search_min)))
+        return fail(TOMO_EINVAL, "line_search_size must be >= 2 and line_search_max above line_search_min");
     if (p->maximum_iterations < 0) return fail(TOMO_EINVAL, "maximum_iterations must be >= 0");
     if (p->type == TOMO_SEARCH_DE && (p->number_pairs < 1 || p->population_size < 2 * p->number_pairs + 2))
         return fail(TOMO_EINVAL, "population too small for the number of difference pairs");
     Run R{*p, min_bound, max_bound, n_param, f, user, report, report_user};
     Rng g(p->seed);
-    const int rc = p->type == TOMO_SEARCH_PS ? particle_swarm(R, g, best_params, best_fitness, history)
-                                             : differential_evolution(R, g, best_params, best_fitness, history);
+    const int rc = p->type == TOMO_SEARCH_PS   ? particle_swarm(R, g, best_params, best_fitness, history)
+                   : p->type == TOMO_SEARCH_DE ? differential_evolution(R, g, best_params, best_fitness, history)
+                                               : newton_method(R, g, best_params, best_fitness, history);
     if (evaluations) *evaluations = R.evals;
     return rc;
 }

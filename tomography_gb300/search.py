@@ -36,7 +36,7 @@ import numpy as np
 
 FitnessFn = Callable[[np.ndarray], np.ndarray]
 
-SEARCH_PS, SEARCH_DE = 0, 1
+SEARCH_PS, SEARCH_DE, SEARCH_ANM = 0, 1, 2
 
 
 from . import BATCH_FN, REPORT_FN, SearchParams  # noqa: E402  (ABI mirrors of include/tomography.h)
@@ -205,6 +205,53 @@ class DifferentialEvolution(_Search):
         return p
 
 
+class NewtonMethod(_Search):
+    """Regression Newton method: each iteration samples ``--regression_size``
+    points within ``radius`` of the best point so far (one batch call), fits a
+    quadratic model by least squares, and evaluates ``--line_search_size``
+    points along the Newton step between ``--line_search_min`` and
+    ``--line_search_max`` times the step (one batch call).  The construction
+    ``(min_bound, max_bound, radius, arguments)`` and ``iterate(f)`` are those of
+    tao's AsynchronousNewtonMethod in the reference's driver (test.cxx:116-121);
+    the search starts at the bounds' midpoint.  ``--hessian_diagonal 1`` fits
+    only the Hessian's diagonal, for many free parameters."""
+
+    TYPE = SEARCH_ANM
+
+    def __init__(self, min_bound, max_bound, radius=None, arguments=None, *, regression_size=None,
+                 line_search_size=None, line_search_min=None, line_search_max=None, hessian_diagonal=None,
+                 maximum_iterations=None, seed=None):
+        super().__init__(min_bound, max_bound, arguments, population_size=4,
+                         maximum_iterations=maximum_iterations or get_argument(arguments, "--maximum_iterations", 10,
+                                                                               int), seed=seed)
+        self.radius = None if radius is None else np.ascontiguousarray(radius, dtype=np.float64)
+        if self.radius is not None and self.radius.shape != self.lo.shape:
+            raise ValueError("radius must have one value per parameter")
+        self.regression_size = int(regression_size if regression_size is not None
+                                   else get_argument(arguments, "--regression_size", 0, int))
+        self.line_search_size = int(line_search_size if line_search_size is not None
+                                    else get_argument(arguments, "--line_search_size", 13, int))
+        self.line_search_min = float(line_search_min if line_search_min is not None
+                                     else get_argument(arguments, "--line_search_min", -1.0))
+        self.line_search_max = float(line_search_max if line_search_max is not None
+                                     else get_argument(arguments, "--line_search_max", 2.0))
+        self.hessian_diagonal = int(hessian_diagonal if hessian_diagonal is not None
+                                    else get_argument(arguments, "--hessian_diagonal", 0, int))
+
+    def _params(self) -> SearchParams:
+        p = super()._params()
+        if self.radius is not None:
+            p.radius = self.radius.ctypes.data_as(C.POINTER(C.c_double))
+        p.regression_size, p.line_search_size = self.regression_size, self.line_search_size
+        p.line_search_min, p.line_search_max = self.line_search_min, self.line_search_max
+        p.hessian_diagonal = self.hessian_diagonal
+        return p
+
+    def iterate(self, f, batch: bool = True, callback=None) -> SearchResult:
+        """tao's name for the Newton method's run (``anm.iterate(FDTD_GPU)``)."""
+        return self.go(f, batch, callback)
+
+
 def breast_bounds(n_ellipses: int, disc_radius: float):
     """Per-parameter bounds of the breast-imaging candidates: 8 per ellipse
     (cx, cy, a, b, angle, eps_inf, delta_eps, sigma)."""
@@ -223,7 +270,7 @@ def reference_bounds():
 def main(argv=None) -> int:
     argv = list(sys.argv[1:] if argv is None else argv)
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
-    ap.add_argument("--search_type", required=True, choices=["ps", "de"])
+    ap.add_argument("--search_type", required=True, choices=["ps", "de", "anm"])
     ap.add_argument("--workload", type=int, default=1, help="breast-imaging workload (0..4)")
     ap.add_argument("--target_seed_offset", type=int, default=1)
     ap.add_argument("--steps", type=int, default=0, help="override the time steps per solve")
@@ -239,7 +286,10 @@ def main(argv=None) -> int:
     with T.Solver(spec.copy(n_ellipses=3)) as ts:
         target = ts.forward(W.target_phantom(args.workload, 3), traces=True, far_field=False)["traces"][0]
     lo, hi = breast_bounds(K, spec.disc_radius)
-    search = (ParticleSwarm if args.search_type == "ps" else DifferentialEvolution)(lo, hi, rest)
+    if args.search_type == "anm":
+        search = NewtonMethod(lo, hi, 0.1 * (hi - lo), rest)
+    else:
+        search = (ParticleSwarm if args.search_type == "ps" else DifferentialEvolution)(lo, hi, rest)
     with T.Solver(spec) as s:
         s.set_target(target)
 
