@@ -266,7 +266,8 @@ typedef struct tomo_search_params {
                                      1 + k + k(k+1)/2 for k free parameters)          */
     int32_t reserved2;
 } tomo_search_params;
-/* fitness[i] of population[i*n_param ...], i < n_cand; non-zero return aborts the search */
+/* fitness[i] of population[i*n_param ...], i < n_cand; non-zero return aborts the
+   search.  A NaN fitness ranks below every number (-infinity). */
 typedef int (*tomo_batch_fitness_fn)(void *user, const double *population, size_t n_cand, size_t n_param,
                                      double *fitness);
 /* called after every generation with the best fitness and parameters so far */

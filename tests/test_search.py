@@ -274,3 +274,26 @@ def test_newton_method_arguments_like_tao():
     bad = S.NewtonMethod(np.zeros(3), np.ones(3), np.ones(3), line_search_size=1)
     with pytest.raises(Exception):
         bad.go(lambda x: -np.sum(x * x, axis=1))
+
+
+@pytest.mark.parametrize("cls", ["ParticleSwarm", "DifferentialEvolution", "NewtonMethod"])
+def test_nan_fitness_ranks_below_every_number(cls):
+    """A candidate whose fitness is NaN (a diverged solve) is never kept as
+    best, even when it is the first one evaluated."""
+    lo, hi = np.full(3, -2.0), np.full(3, 2.0)
+    first = [True]
+
+    def f(x):
+        v = -np.sum((x - 0.3) ** 2, axis=1)
+        if first[0]:
+            v[0] = np.nan   # the first candidate of the first batch
+            first[0] = False
+        v[np.abs(x[:, 1]) > 1.9] = np.nan
+        return v
+
+    kw = dict(maximum_iterations=30, seed=5)
+    s = (S.NewtonMethod(lo, hi, np.full(3, 0.5), **kw) if cls == "NewtonMethod"
+         else getattr(S, cls)(lo, hi, population_size=20, **kw))
+    res = s.go(f)
+    assert np.isfinite(res.best_fitness) and res.best_fitness > -0.05
+    assert np.all(np.isfinite(res.history[1:]))

@@ -69,10 +69,14 @@ struct Run {
     void* report_user;
     int64_t evals = 0;
 
+    // a NaN fitness (a diverged or failed candidate) ranks below every number,
+    // so that no comparison of the drivers can keep or prefer it
     int evaluate(const std::vector<double>& x, size_t n, std::vector<double>& fx) {
         fx.assign(n, 0.0);
         const int rc = f(user, x.data(), n, np, fx.data());
         if (rc != TOMO_OK) return rc;
+        for (double& v : fx)
+            if (std::isnan(v)) v = -HUGE_VAL;
         evals += (int64_t)n;
         return TOMO_OK;
     }
@@ -82,7 +86,7 @@ struct Run {
 size_t argmax(const std::vector<double>& v) {
     size_t b = 0;
     for (size_t i = 1; i < v.size(); ++i)
-        if (v[i] > v[b]) b = i;   // NaN never wins
+        if (v[i] > v[b]) b = i;
     return b;
 }
 
