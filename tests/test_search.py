@@ -127,6 +127,36 @@ def test_search_fitness_over_a_handle(tomo):
     assert np.all(best >= lo) and np.all(best <= hi)
 
 
+@pytest.mark.gpu
+def test_newton_method_over_gpu_fitness(tomo):
+    """The Newton driver over Solver.fitness_batch (test.cxx:116-121's
+    anm.iterate(FDTD_GPU) shape): the start point, the regression sample and
+    the line search are one batch each; the best point re-evaluates to its
+    fitness and is no worse than the start."""
+    from helpers import small_breast_spec, small_params
+    from tomography_gb300 import workloads as W
+
+    spec = small_breast_spec(tomo, n_ellipses=2)
+    with tomo.Solver(spec.copy(n_ellipses=3)) as ts:
+        target = ts.forward(small_params(W, 3), traces=True, far_field=False)["traces"][0]
+    lo, hi = S.breast_bounds(2, spec.disc_radius)
+    sizes = []
+    with tomo.Solver(spec) as s:
+        s.set_target(target)
+
+        def f(x):
+            sizes.append(x.shape[0])
+            return s.fitness_batch(x)
+
+        res = S.NewtonMethod(lo, hi, 0.1 * (hi - lo), hessian_diagonal=1, regression_size=40,
+                             maximum_iterations=1, seed=3).iterate(f)
+        again = s.fitness(res.best_params)
+    assert sizes == [1, 40, 13] and res.evaluations == 54
+    assert np.isfinite(res.best_fitness) and again == res.best_fitness
+    assert res.history[1] >= res.history[0]
+    assert np.all(res.best_params >= lo) and np.all(res.best_params <= hi)
+
+
 def test_search_argument_errors(tomo):
     """tao-style arguments: unknown names are skipped, a malformed value or an
     unknown parent selection is refused; bounds with min > max are refused."""
