@@ -33,7 +33,7 @@
   computes what the source intends.
 
 Sources are read from the reference tree named by the environment variable
-``TOMO_REFERENCE_TREE`` (default: the tree this build was set up with), or,
+``TOMO_REFERENCE_TREE`` (default: the checkout path below), or,
 where that tree is absent, from the staged copy.  Nothing in the product
 imports this module; ``__graft_entry__.build()`` calls it so that the checker
 exists wherever the tests run.
