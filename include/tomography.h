@@ -282,7 +282,10 @@ int tomo_search_parse_args(tomo_search_params *p, int argc, const char *const *a
 int tomo_search_run(const tomo_search_params *p, const double *min_bound, const double *max_bound, size_t n_param,
                     tomo_batch_fitness_fn f, void *user, tomo_generation_fn report, void *report_user,
                     double *best_params, double *best_fitness, double *history, int64_t *evaluations);
-/* the same with tomo_fitness_batch of the handle as f (tomo_num_params parameters) */
+/* the same with tomo_fitness_batch of the handle as f (tomo_num_params
+   parameters).  A candidate whose solve diverges (non-finite fitness, which
+   tomo_fitness_batch reports as TOMO_ENUMERIC) ranks below every number and
+   the search goes on; best_fitness is -infinity when every candidate diverged. */
 int tomo_search_fitness(tomo_handle *h, const tomo_search_params *p, const double *min_bound,
                         const double *max_bound, tomo_generation_fn report, void *report_user, double *best_params,
                         double *best_fitness, double *history);

@@ -76,3 +76,38 @@ def test_poisoned_request_is_rejected_at_submit(tomo):
             s.serve_step()
             got = s.poll(t, 1)
         assert got[0] == s.fitness(good)
+
+
+def test_search_over_a_handle_ranks_diverged_candidates_last(tomo):
+    """tomo_search_fitness goes on past a diverged candidate: its fitness is
+    non-finite and ranks below every number.  Ellipse 0 is held at the
+    unstable permittivity above (min == max), so every candidate diverges and
+    the search ends with TOMO_OK and a best fitness of -infinity; the same
+    search with that ellipse stable finds a finite best."""
+    import ctypes as C
+
+    from tomography_gb300 import search as S
+    from tomography_gb300 import workloads as W
+
+    spec = small_breast_spec(tomo, n_ellipses=3, steps=300)
+    good = small_params(W, 3, seed_offset=7)
+    lib = tomo.library()
+    dp = C.POINTER(C.c_double)
+    with tomo.Solver(spec) as s:
+        s.set_target(s.forward(small_params(W, 3), traces=True, far_field=False)["traces"][0])
+        results = []
+        for eps in (0.01, float(good[5])):
+            lo, hi = S.breast_bounds(3, spec.disc_radius)
+            lo[:8] = hi[:8] = good[:8]
+            lo[5] = hi[5] = eps
+            p = tomo.SearchParams()
+            assert lib.tomo_search_defaults(C.byref(p), S.SEARCH_PS) == 0
+            p.population_size, p.maximum_iterations, p.seed = 4, 1, 3
+            best, fit = np.zeros(lo.size), C.c_double()
+            rc = lib.tomo_search_fitness(s._h, C.byref(p), lo.ctypes.data_as(dp), hi.ctypes.data_as(dp),
+                                         tomo.REPORT_FN(), None, best.ctypes.data_as(dp), C.byref(fit), None)
+            assert rc == 0, lib.tomo_last_error()
+            results.append(fit.value)
+        assert results[0] == -np.inf
+        assert np.isfinite(results[1])
+        assert s.fitness(good) == s.fitness(good)   # the handle is still usable

@@ -125,9 +125,13 @@ int tomo_wait(tomo_handle* h, uint64_t ticket, double timeout_ms, double* fitnes
 }
 
 // tomo_search_fitness: the search drivers of search.cpp with the handle's
-// batch fitness (tomo_fitness_batch) as the generation evaluator
+// batch fitness (tomo_fitness_batch) as the generation evaluator.  A candidate
+// whose solve diverges has a non-finite fitness (TOMO_ENUMERIC, every fitness
+// written); the drivers rank it below every number and the search goes on, as
+// the reference's search goes on past its clamped fields.
 static int handle_fitness(void* user, const double* pop, size_t n, size_t np, double* fit) {
-    return tomo_fitness_batch(static_cast<tomo_handle*>(user), pop, n, np, fit);
+    const int rc = tomo_fitness_batch(static_cast<tomo_handle*>(user), pop, n, np, fit);
+    return rc == TOMO_ENUMERIC ? TOMO_OK : rc;
 }
 
 int tomo_search_fitness(tomo_handle* h, const tomo_search_params* p, const double* min_bound,
