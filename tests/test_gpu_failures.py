@@ -111,3 +111,26 @@ def test_search_over_a_handle_ranks_diverged_candidates_last(tomo):
         assert results[0] == -np.inf
         assert np.isfinite(results[1])
         assert s.fitness(good) == s.fitness(good)   # the handle is still usable
+
+
+def test_python_search_over_a_solver_keeps_going(tomo):
+    """Solver.fitness_batch(diverged="keep") returns a diverged candidate's
+    non-finite fitness beside the others'; a Python search given the Solver
+    itself ranks diverged candidates last, as tomo_search_fitness does."""
+    from tomography_gb300 import search as S
+    from tomography_gb300 import workloads as W
+
+    spec = small_breast_spec(tomo, n_ellipses=3, steps=300)
+    good = small_params(W, 3, seed_offset=7)
+    unstable = good.copy()
+    unstable[5] = 0.01
+    with tomo.Solver(spec) as s:
+        s.set_target(s.forward(small_params(W, 3), traces=True, far_field=False)["traces"][0])
+        with pytest.raises(tomo.TomoError):
+            s.fitness_batch(np.stack([good, unstable]))
+        f = s.fitness_batch(np.stack([good, unstable]), diverged="keep")
+        assert f[0] == s.fitness(good) and not np.isfinite(f[1])
+        lo, hi = S.breast_bounds(3, spec.disc_radius)
+        lo[:8] = hi[:8] = unstable[:8]
+        res = S.ParticleSwarm(lo, hi, population_size=4, maximum_iterations=1, seed=3).go(s)
+        assert res.best_fitness == -np.inf and res.evaluations == 8

@@ -27,6 +27,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libtomography_gb300.so")
 
 TOMO_OK = 0
+TOMO_ENUMERIC = -4
 STATUS_NAMES = {
     -1: "TOMO_EINVAL",
     -2: "TOMO_ENOMEM_BUDGET",
@@ -266,11 +267,20 @@ class Solver:
         _check(library().tomo_fitness(self._h, _dptr(a), a.shape[1], _dptr(out)))
         return float(out[0])
 
-    def fitness_batch(self, args, out: Optional[np.ndarray] = None) -> np.ndarray:
+    def fitness_batch(self, args, out: Optional[np.ndarray] = None, *, diverged: str = "raise") -> np.ndarray:
+        """Fitness of every candidate of ``args`` ([n_cand, n_params]).  A
+        candidate whose solve diverges has a non-finite fitness: ``diverged=
+        "raise"`` raises TomoError(TOMO_ENUMERIC); ``"keep"`` returns every
+        fitness, the diverged ones non-finite (what a search wants: the
+        reference's search goes on past a clamped field)."""
+        if diverged not in ("raise", "keep"):
+            raise ValueError("diverged must be 'raise' or 'keep'")
         a = self._args(args)
         if out is None:
             out = np.zeros(a.shape[0], dtype=np.float64)
-        _check(library().tomo_fitness_batch(self._h, _dptr(a), a.shape[0], a.shape[1], _dptr(out)))
+        rc = library().tomo_fitness_batch(self._h, _dptr(a), a.shape[0], a.shape[1], _dptr(out))
+        if not (rc == TOMO_ENUMERIC and diverged == "keep"):
+            _check(rc)
         return out
 
     def forward(self, args, traces: bool = True, far_field: bool = True, fitness: bool = False,

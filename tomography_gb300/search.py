@@ -1,12 +1,14 @@
-"""Synchronous particle-swarm and differential-evolution drivers over whole
-generations: Python face of the library's C++ drivers (csrc/search.cpp,
+"""Synchronous particle-swarm, differential-evolution and regression Newton
+drivers over whole generations: Python face of the library's C++ drivers (csrc/search.cpp,
 ``tomo_search_run`` in include/tomography.h; C++ callers use
 include/tomography_search.hpp).
 
 The reference hands its fitness function to tao's searches as a function
 pointer (test.cxx:82-121): ``ParticleSwarmMPI ps(min_bound, max_bound,
 arguments); ps.go(FDTD_GPU)``, ``DifferentialEvolutionMPI de(...);
-de.go(...)``, with tao farming one candidate per MPI rank and call.  tao itself
+de.go(...)``, ``AsynchronousNewtonMethod anm(min_bound, max_bound, radius,
+arguments); anm.iterate(FDTD_GPU)``, with tao farming one candidate per MPI
+rank and call.  tao itself
 is an un-vendored submodule, so the drivers restate the textbook synchronous
 algorithms with the same construction and ``go(f)`` call shape, and evaluate
 every generation in ONE call: ``f`` receives the whole population as an
@@ -103,9 +105,17 @@ class _Search:
 
     def go(self, f, batch: bool = True, callback=None) -> SearchResult:
         """Run the search; ``f`` evaluates a whole generation (``batch=True``)
-        or one candidate given as a list (``batch=False``)."""
-        from . import library
+        or one candidate given as a list (``batch=False``).  ``f`` may be a
+        ``Solver``: its batch fitness, with a diverged candidate's non-finite
+        fitness ranked below every number instead of raised (the rule of
+        ``tomo_search_fitness``)."""
+        from . import Solver, library
 
+        if isinstance(f, Solver):
+            if f.n_params != self.n_param:
+                raise ValueError(f"the solver takes {f.n_params} parameters, the bounds give {self.n_param}")
+            solver = f
+            f, batch = (lambda x: solver.fitness_batch(x, diverged="keep")), True
         ev = self._evaluator(f, batch)
         errors = []
 
@@ -296,7 +306,7 @@ def main(argv=None) -> int:
         def report(it, best, _):
             print(json.dumps({"generation": it, "best_fitness": best}), flush=True)
 
-        res = search.go(s.fitness_batch, callback=report)
+        res = search.go(s, callback=report)
     print(json.dumps({"search_type": args.search_type, "best_fitness": res.best_fitness,
                       "evaluations": res.evaluations, "generations": res.generations, "seconds": res.seconds,
                       "evals_per_s": res.evaluations / res.seconds}))
