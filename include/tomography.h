@@ -183,7 +183,9 @@ int tomo_set_target_spec(tomo_handle *h, const tomo_spec *spec, const float *tar
 int tomo_request_bytes(tomo_handle *h, const tomo_spec *spec, size_t n_cand, uint64_t *bytes);
 /* advance every admitted solve by one launch; admits queued work first          */
 int tomo_serve_step(tomo_handle *h, int *n_active);
-/* fitness of a finished ticket (n_cand values), TOMO_ENOTREADY while running    */
+/* fitness of a finished ticket (n_cand values), TOMO_ENOTREADY while running.
+   A finished, failed or cancelled ticket is reported once (TOMO_OK or its
+   status, TOMO_ECANCELLED), then forgotten: polling it again is TOMO_EINVAL.  */
 int tomo_poll(tomo_handle *h, uint64_t ticket, double *fitness);
 /* bounded wait for one ticket: runs tomo_serve_step until the ticket has
    finished (its result as tomo_poll) or timeout_ms has passed, checked before

@@ -160,6 +160,9 @@ def test_cancel(tomo):
         with pytest.raises(tomo.TomoError) as ei:
             s.poll(t2, 2)
         assert ei.value.status == -7   # TOMO_ECANCELLED
+        with pytest.raises(tomo.TomoError) as ei:
+            s.poll(t2, 2)              # reported once, then forgotten
+        assert ei.value.status == -1
 
 
 def test_bounded_wait(tomo):

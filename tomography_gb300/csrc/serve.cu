@@ -430,7 +430,10 @@ int EngineT<Real>::poll(uint64_t ticket, double* fitness) {
     auto it = serve_->reqs.find(ticket);
     if (it == serve_->reqs.end()) return fail(TOMO_EINVAL, "unknown ticket");
     ServeRequest<Real>& r = *it->second;
-    if (r.state == kCancelled) return fail(TOMO_ECANCELLED, "ticket was cancelled");
+    if (r.state == kCancelled) {
+        serve_->reqs.erase(it);   // reported once, then forgotten
+        return fail(TOMO_ECANCELLED, "ticket was cancelled");
+    }
     if (r.state == kFailed) {
         const int status = r.status;
         serve_->reqs.erase(it);   // reported once, then forgotten like a finished request
@@ -454,7 +457,10 @@ int EngineT<Real>::cancel(uint64_t ticket) {
         TOMO_TRY(retire(serve_, r, stream_, false));
         CUDA_TRY(cudaStreamSynchronize(stream_));
     }
-    if (r.state == kQueued || r.state == kRunning) r.state = kCancelled;
+    if (r.state == kQueued || r.state == kRunning) {
+        r.state = kCancelled;
+        r.up = Unpacked{};   // only the ticket's state is kept until it is polled
+    }
     return TOMO_OK;
 }
 
