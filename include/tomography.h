@@ -33,7 +33,8 @@ typedef enum tomo_status {
     TOMO_ECUDA = -5,           /* CUDA runtime error (the reference calls exit(-1))      */
     TOMO_ENOTREADY = -6,       /* serving ticket not finished yet                        */
     TOMO_ECANCELLED = -7,      /* serving ticket was cancelled                           */
-    TOMO_ENOTARGET = -8        /* fitness requested before a target was set              */
+    TOMO_ENOTARGET = -8,       /* fitness requested before a target was set              */
+    TOMO_ENOMEM_HOST = -9      /* a host allocation failed (no C++ exception crosses the ABI) */
 } tomo_status;
 
 typedef enum tomo_mode {

@@ -327,3 +327,31 @@ def test_nan_fitness_ranks_below_every_number(cls):
     res = s.go(f)
     assert np.isfinite(res.best_fitness) and res.best_fitness > -0.05
     assert np.all(np.isfinite(res.history[1:]))
+
+
+def test_no_cpp_exception_crosses_the_c_abi(tomo):
+    """A host allocation that cannot succeed (a 2^31-member swarm over 10^6
+    parameters: 17 PB) returns TOMO_ENOMEM_HOST instead of aborting the
+    caller; a full Newton model too large to solve is refused up front."""
+    import ctypes as C
+
+    lib = tomo.library()
+    p = tomo.SearchParams()
+    assert lib.tomo_search_defaults(C.byref(p), S.SEARCH_PS) == 0
+    p.population_size, p.maximum_iterations = 2 ** 31 - 1, 1
+    n = 10 ** 6
+    lo, hi = np.zeros(n), np.ones(n)
+    dp = C.POINTER(C.c_double)
+    best, fit = np.zeros(n), C.c_double()
+    called = []
+    cb = tomo.BATCH_FN(lambda u, pop, m, npar, out: called.append(m) or 0)
+    rc = lib.tomo_search_run(C.byref(p), lo.ctypes.data_as(dp), hi.ctypes.data_as(dp), n, cb, None, tomo.REPORT_FN(),
+                             None, best.ctypes.data_as(dp), C.byref(fit), None, None)
+    assert rc == -9 and not called                     # TOMO_ENOMEM_HOST
+    assert "allocation" in lib.tomo_last_error().decode()
+    with pytest.raises(Exception, match="hessian_diagonal"):
+        S.NewtonMethod(np.zeros(200), np.ones(200), np.full(200, 0.1), maximum_iterations=1).go(
+            lambda x: -np.sum(x * x, axis=1))
+    ok = S.NewtonMethod(np.zeros(200), np.ones(200), np.full(200, 0.1), hessian_diagonal=1, regression_size=450,
+                        maximum_iterations=1).go(lambda x: -np.sum((x - 0.5) ** 2, axis=1))
+    assert ok.best_fitness > -1e-6

@@ -37,6 +37,7 @@ STATUS_NAMES = {
     -6: "TOMO_ENOTREADY",
     -7: "TOMO_ECANCELLED",
     -8: "TOMO_ENOTARGET",
+    -9: "TOMO_ENOMEM_HOST",
 }
 
 

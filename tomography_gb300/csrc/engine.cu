@@ -876,14 +876,16 @@ int create_engine(const tomo_spec* spec, EngineBase** out) {
 // the item count, or a negative status.
 extern "C" int tomo_internal_work_items(int nx, int ny, int ncpml, int d, int T, int cols, int nseg, int* out,
                                         int cap) {
-    std::vector<tomo::WorkItem> items;
-    tomo::append_items(items, 0, 1, nx, ny, ncpml, d, T, cols, nseg);
-    TOMO_TRY(tomo::validate_items(items, 0, nx, ny, ncpml, d, T, cols));
-    if (!out || (int)items.size() > cap) return tomo::fail(TOMO_EINVAL, "item buffer too small");
-    for (size_t i = 0; i < items.size(); ++i) {
-        const tomo::WorkItem& w = items[i];
-        const int rec[5] = {w.x0, w.x1, w.narrow, w.y0, w.y1};
-        for (int j = 0; j < 5; ++j) out[5 * i + j] = rec[j];
-    }
-    return (int)items.size();
+    return tomo::guarded([&]() -> int {
+        std::vector<tomo::WorkItem> items;
+        tomo::append_items(items, 0, 1, nx, ny, ncpml, d, T, cols, nseg);
+        TOMO_TRY(tomo::validate_items(items, 0, nx, ny, ncpml, d, T, cols));
+        if (!out || (int)items.size() > cap) return tomo::fail(TOMO_EINVAL, "item buffer too small");
+        for (size_t i = 0; i < items.size(); ++i) {
+            const tomo::WorkItem& w = items[i];
+            const int rec[5] = {w.x0, w.x1, w.narrow, w.y0, w.y1};
+            for (int j = 0; j < 5; ++j) out[5 * i + j] = rec[j];
+        }
+        return (int)items.size();
+    });
 }

@@ -1,5 +1,7 @@
 // Internal engine interface behind the C ABI.
 #pragma once
+#include <new>
+#include <stdexcept>
 #include <string>
 #include "../../include/tomography.h"
 
@@ -25,6 +27,34 @@ class EngineBase {
 
 int fail(int code, const std::string& msg);
 extern thread_local std::string g_last_error;
+
+// The same as fail() without throwing: for the error paths of guarded().
+inline int fail_noexcept(int code, const char* msg) noexcept {
+    try {
+        g_last_error = msg;
+    } catch (...) {
+        g_last_error.clear();
+    }
+    return code;
+}
+
+// Body of a C ABI entry point: no C++ exception crosses into a C (or ctypes)
+// caller.  A host allocation failure is TOMO_ENOMEM_HOST, any other exception
+// TOMO_EINVAL, with the reason in tomo_last_error().
+template <class Body>
+int guarded(Body&& body) noexcept {
+    try {
+        return body();
+    } catch (const std::bad_alloc&) {
+        return fail_noexcept(TOMO_ENOMEM_HOST, "host memory allocation failed");
+    } catch (const std::length_error& e) {
+        return fail_noexcept(TOMO_ENOMEM_HOST, e.what());
+    } catch (const std::exception& e) {
+        return fail_noexcept(TOMO_EINVAL, e.what());
+    } catch (...) {
+        return fail_noexcept(TOMO_EINVAL, "unexpected exception");
+    }
+}
 
 int spec_reference(tomo_spec* s, int cpu_variant);
 int spec_breast(tomo_spec* s, int config);

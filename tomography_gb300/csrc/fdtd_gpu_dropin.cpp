@@ -109,21 +109,24 @@ size_t reference_target_size() {
     return (size_t)spec.n_excitations * spec.nfreq * spec.n_angles;
 }
 
-tomo_handle* handle_locked() {
-    if (g_handle) return g_handle;
-    tomo_spec spec;
-    int rc = tomo_spec_reference(&spec, 0);
-    if (rc) throw_status(rc, "tomo_spec_reference");
-    rc = tomo_create(&spec, &g_handle);
-    if (rc) throw_status(rc, "tomo_create");
-    return g_handle;
+// the process-wide handle, created on first use (caller holds g_mu)
+int handle_locked(tomo_handle** h) {
+    if (!g_handle) {
+        tomo_spec spec;
+        int rc = tomo_spec_reference(&spec, 0);
+        if (rc == TOMO_OK) rc = tomo_create(&spec, &g_handle);
+        if (rc) return rc;
+    }
+    *h = g_handle;
+    return TOMO_OK;
 }
 
 }  // namespace
 
 double FDTD_GPU(const std::vector<double>& arguments) {
     std::lock_guard<std::mutex> lock(g_mu);
-    tomo_handle* h = handle_locked();
+    tomo_handle* h = nullptr;
+    if (int rc = handle_locked(&h)) throw_status(rc, "tomo_create");
     tomo_spec spec;
     tomo_spec_reference(&spec, 0);
     const size_t need = (size_t)tomo_num_params(&spec);
@@ -147,18 +150,17 @@ double FDTD_GPU(const std::vector<double>& arguments) {
 }
 
 extern "C" int tomo_fdtd_gpu_set_target(const float* target, size_t n) {
-    std::lock_guard<std::mutex> lock(g_mu);
-    std::vector<float> t;
-    std::string why;
-    if (target_values(target, n, reference_target_size(), t, why)) return tomo::fail(TOMO_EINVAL, why);
-    try {
-        tomo_handle* h = handle_locked();
-        int rc = tomo_set_target(h, t.data(), t.size());
+    return tomo::guarded([&]() -> int {
+        std::lock_guard<std::mutex> lock(g_mu);
+        std::vector<float> t;
+        std::string why;
+        if (target_values(target, n, reference_target_size(), t, why)) return tomo::fail(TOMO_EINVAL, why);
+        tomo_handle* h = nullptr;
+        int rc = handle_locked(&h);
+        if (rc == TOMO_OK) rc = tomo_set_target(h, t.data(), t.size());
         if (rc == TOMO_OK) g_target_set = true;
         return rc;
-    } catch (const std::exception&) {
-        return TOMO_ECUDA;
-    }
+    });
 }
 
 // Internal test hook (not part of the public ABI): the target the drop-in
@@ -166,14 +168,16 @@ extern "C" int tomo_fdtd_gpu_set_target(const float* target, size_t n) {
 // rules as TOMO_MEASUREMENT_FILE), copied into out[0..cap).  Returns the
 // number of values, or a negative status with the reason in tomo_last_error().
 extern "C" int tomo_internal_read_target_file(const char* path, float* out, size_t cap) {
-    std::vector<float> raw, t;
-    std::string why;
-    if (!path) return tomo::fail(TOMO_EINVAL, "NULL path");
-    if (read_target_file(path, raw, why) || target_values(raw.data(), raw.size(), reference_target_size(), t, why))
-        return tomo::fail(TOMO_EINVAL, why);
-    if (!out || cap < t.size()) return tomo::fail(TOMO_EINVAL, "output buffer too small");
-    std::copy(t.begin(), t.end(), out);
-    return (int)t.size();
+    return tomo::guarded([&]() -> int {
+        std::vector<float> raw, t;
+        std::string why;
+        if (!path) return tomo::fail(TOMO_EINVAL, "NULL path");
+        if (read_target_file(path, raw, why) || target_values(raw.data(), raw.size(), reference_target_size(), t, why))
+            return tomo::fail(TOMO_EINVAL, why);
+        if (!out || cap < t.size()) return tomo::fail(TOMO_EINVAL, "output buffer too small");
+        std::copy(t.begin(), t.end(), out);
+        return (int)t.size();
+    });
 }
 
 extern "C" void tomo_fdtd_gpu_release(void) {

@@ -51,47 +51,49 @@ using tomo::fail;
 
 extern "C" int tomo_trace_misfit_static(const float* traces, const float* target, size_t n_cand, size_t n_tx,
                                         size_t n_per_solve, double* fitness, void* stream) {
-    if (!traces || !target || !fitness) return fail(TOMO_EINVAL, "tomo_trace_misfit_static: NULL buffer");
-    if (n_cand == 0 || n_tx == 0 || n_per_solve == 0)
-        return fail(TOMO_EINVAL, "tomo_trace_misfit_static: empty problem");
-    if (n_cand > tomo::kNoAllocMaxSolves || n_tx > tomo::kNoAllocMaxSolves ||
-        n_cand * n_tx > tomo::kNoAllocMaxSolves)
-        return fail(TOMO_EINVAL, "tomo_trace_misfit_static: " + std::to_string(n_cand) + " x " + std::to_string(n_tx) +
-                                     " solves exceed the static scratch limit of " +
-                                     std::to_string(tomo::kNoAllocMaxSolves) + " solves");
-    if (n_per_solve > (size_t)0x7fffffff) return fail(TOMO_EINVAL, "tomo_trace_misfit_static: trace too long");
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return fail(TOMO_ECUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-    if (dev < 0 || dev >= tomo::kMaxDevices) return fail(TOMO_ECUDA, "device index out of range");
-    double* partials = nullptr;
-    int* flag = nullptr;
-    {
-        std::lock_guard<std::mutex> lock(tomo::g_mu);
-        if (!tomo::g_partials_addr[dev]) {
-            // one-time set-up per device, with that device current
-            void* p = nullptr;
-            e = cudaGetSymbolAddress(&p, tomo::g_misfit_partials);
-            if (e != cudaSuccess)
-                return fail(TOMO_ECUDA, std::string("cudaGetSymbolAddress(partials): ") + cudaGetErrorString(e));
-            void* q = nullptr;
-            e = cudaGetSymbolAddress(&q, tomo::g_misfit_flag);
-            if (e != cudaSuccess)
-                return fail(TOMO_ECUDA, std::string("cudaGetSymbolAddress(flag): ") + cudaGetErrorString(e));
-            tomo::g_partials_addr[dev] = static_cast<double*>(p);
-            tomo::g_flag_addr[dev] = static_cast<int*>(q);
+    return tomo::guarded([&]() -> int {
+        if (!traces || !target || !fitness) return fail(TOMO_EINVAL, "tomo_trace_misfit_static: NULL buffer");
+        if (n_cand == 0 || n_tx == 0 || n_per_solve == 0)
+            return fail(TOMO_EINVAL, "tomo_trace_misfit_static: empty problem");
+        if (n_cand > tomo::kNoAllocMaxSolves || n_tx > tomo::kNoAllocMaxSolves ||
+            n_cand * n_tx > tomo::kNoAllocMaxSolves)
+            return fail(TOMO_EINVAL, "tomo_trace_misfit_static: " + std::to_string(n_cand) + " x " + std::to_string(n_tx) +
+                                         " solves exceed the static scratch limit of " +
+                                         std::to_string(tomo::kNoAllocMaxSolves) + " solves");
+        if (n_per_solve > (size_t)0x7fffffff) return fail(TOMO_EINVAL, "tomo_trace_misfit_static: trace too long");
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e != cudaSuccess) return fail(TOMO_ECUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+        if (dev < 0 || dev >= tomo::kMaxDevices) return fail(TOMO_ECUDA, "device index out of range");
+        double* partials = nullptr;
+        int* flag = nullptr;
+        {
+            std::lock_guard<std::mutex> lock(tomo::g_mu);
+            if (!tomo::g_partials_addr[dev]) {
+                // one-time set-up per device, with that device current
+                void* p = nullptr;
+                e = cudaGetSymbolAddress(&p, tomo::g_misfit_partials);
+                if (e != cudaSuccess)
+                    return fail(TOMO_ECUDA, std::string("cudaGetSymbolAddress(partials): ") + cudaGetErrorString(e));
+                void* q = nullptr;
+                e = cudaGetSymbolAddress(&q, tomo::g_misfit_flag);
+                if (e != cudaSuccess)
+                    return fail(TOMO_ECUDA, std::string("cudaGetSymbolAddress(flag): ") + cudaGetErrorString(e));
+                tomo::g_partials_addr[dev] = static_cast<double*>(p);
+                tomo::g_flag_addr[dev] = static_cast<int*>(q);
+            }
+            partials = tomo::g_partials_addr[dev];
+            flag = tomo::g_flag_addr[dev];
         }
-        partials = tomo::g_partials_addr[dev];
-        flag = tomo::g_flag_addr[dev];
-    }
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const int nsolves = (int)(n_cand * n_tx);
-    e = cudaMemsetAsync(flag, 0, sizeof(int) * 4, st);   // the flag must start at zero every call
-    if (e != cudaSuccess) return fail(TOMO_ECUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
-    tomo::trace_partials_kernel<float><<<nsolves, 256, 0, st>>>(traces, n_per_solve, target, (int)n_per_solve,
-                                                                (int)n_tx, 0, partials, flag);
-    tomo::trace_fitness_kernel<<<(int)((n_cand + 127) / 128), 128, 0, st>>>(partials, (int)n_tx, (int)n_cand, fitness);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return fail(TOMO_ECUDA, std::string("misfit launch: ") + cudaGetErrorString(e));
-    return TOMO_OK;
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        const int nsolves = (int)(n_cand * n_tx);
+        e = cudaMemsetAsync(flag, 0, sizeof(int) * 4, st);   // the flag must start at zero every call
+        if (e != cudaSuccess) return fail(TOMO_ECUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
+        tomo::trace_partials_kernel<float><<<nsolves, 256, 0, st>>>(traces, n_per_solve, target, (int)n_per_solve,
+                                                                    (int)n_tx, 0, partials, flag);
+        tomo::trace_fitness_kernel<<<(int)((n_cand + 127) / 128), 128, 0, st>>>(partials, (int)n_tx, (int)n_cand, fitness);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return fail(TOMO_ECUDA, std::string("misfit launch: ") + cudaGetErrorString(e));
+        return TOMO_OK;
+    });
 }

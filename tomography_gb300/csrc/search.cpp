@@ -229,6 +229,12 @@ int newton_method(Run& R, Rng& g, double* best_params, double* best_fitness, dou
     const size_t k = act.size();
     const bool diag = R.p.hessian_diagonal != 0;
     const size_t nq = diag ? k : k * (k + 1) / 2, nu = 1 + k + nq;
+    // the normal equations hold nu^2 doubles and take O(nu^3) to solve
+    constexpr size_t kMaxModelTerms = 8192;
+    if (nu > kMaxModelTerms)
+        return fail(TOMO_EINVAL, "the quadratic model of " + std::to_string(k) + " free parameters has " +
+                                     std::to_string(nu) + " terms (at most " + std::to_string(kMaxModelTerms) +
+                                     "); use --hessian_diagonal 1");
     const size_t m = R.p.regression_size > 0 ? (size_t)R.p.regression_size : std::max<size_t>(2 * nu, nu + 4);
     const size_t L = (size_t)R.p.line_search_size;
     std::vector<double> rad(P);
@@ -315,89 +321,95 @@ int newton_method(Run& R, Rng& g, double* best_params, double* best_fitness, dou
 extern "C" {
 
 int tomo_search_defaults(tomo_search_params* p, int type) {
-    if (!p) return fail(TOMO_EINVAL, "tomo_search_defaults: NULL params");
-    if (type != TOMO_SEARCH_PS && type != TOMO_SEARCH_DE && type != TOMO_SEARCH_ANM)
-        return fail(TOMO_EINVAL, "unknown search type");
-    std::memset(p, 0, sizeof(*p));
-    p->type = type;
-    p->population_size = 50;
-    p->maximum_iterations = 100;
-    p->seed = 0x70F00001ULL;
-    p->inertia = 0.75;
-    p->local_best_weight = 1.5;
-    p->global_best_weight = 1.5;
-    p->crossover_rate = 0.5;
-    p->differential_scale = 0.5;
-    p->number_pairs = 1;
-    p->parent_best = 1;
-    p->radius = nullptr;
-    p->regression_size = 0;
-    p->line_search_size = 13;   // a step of 0.25 over [-1, 2]: the full Newton step a = 1 is one of them
-    p->line_search_min = -1.0;
-    p->line_search_max = 2.0;
-    p->hessian_diagonal = 0;
-    if (type == TOMO_SEARCH_ANM) p->maximum_iterations = 10;
-    return TOMO_OK;
+    return tomo::guarded([&]() -> int {
+        if (!p) return fail(TOMO_EINVAL, "tomo_search_defaults: NULL params");
+        if (type != TOMO_SEARCH_PS && type != TOMO_SEARCH_DE && type != TOMO_SEARCH_ANM)
+            return fail(TOMO_EINVAL, "unknown search type");
+        std::memset(p, 0, sizeof(*p));
+        p->type = type;
+        p->population_size = 50;
+        p->maximum_iterations = 100;
+        p->seed = 0x70F00001ULL;
+        p->inertia = 0.75;
+        p->local_best_weight = 1.5;
+        p->global_best_weight = 1.5;
+        p->crossover_rate = 0.5;
+        p->differential_scale = 0.5;
+        p->number_pairs = 1;
+        p->parent_best = 1;
+        p->radius = nullptr;
+        p->regression_size = 0;
+        p->line_search_size = 13;   // a step of 0.25 over [-1, 2]: the full Newton step a = 1 is one of them
+        p->line_search_min = -1.0;
+        p->line_search_max = 2.0;
+        p->hessian_diagonal = 0;
+        if (type == TOMO_SEARCH_ANM) p->maximum_iterations = 10;
+        return TOMO_OK;
+    });
 }
 
 int tomo_search_parse_args(tomo_search_params* p, int argc, const char* const* argv) {
-    if (!p || argc < 0 || (argc > 0 && !argv)) return fail(TOMO_EINVAL, "tomo_search_parse_args: NULL argument");
-    for (int i = 0; i + 1 < argc; ++i) {
-        const std::string a = argv[i] ? argv[i] : "";
-        const char* v = argv[i + 1];
-        if (!v) continue;
-        char* end = nullptr;
-        if (a == "--population_size") p->population_size = (int32_t)std::strtol(v, &end, 10);
-        else if (a == "--maximum_iterations") p->maximum_iterations = (int32_t)std::strtol(v, &end, 10);
-        else if (a == "--seed") p->seed = (uint64_t)std::strtoull(v, &end, 0);
-        else if (a == "--inertia") p->inertia = std::strtod(v, &end);
-        else if (a == "--local_best_weight") p->local_best_weight = std::strtod(v, &end);
-        else if (a == "--global_best_weight") p->global_best_weight = std::strtod(v, &end);
-        else if (a == "--crossover_rate") p->crossover_rate = std::strtod(v, &end);
-        else if (a == "--differential_scale") p->differential_scale = std::strtod(v, &end);
-        else if (a == "--number_pairs") p->number_pairs = (int32_t)std::strtol(v, &end, 10);
-        else if (a == "--regression_size") p->regression_size = (int32_t)std::strtol(v, &end, 10);
-        else if (a == "--line_search_size") p->line_search_size = (int32_t)std::strtol(v, &end, 10);
-        else if (a == "--line_search_min") p->line_search_min = std::strtod(v, &end);
-        else if (a == "--line_search_max") p->line_search_max = std::strtod(v, &end);
-        else if (a == "--hessian_diagonal") p->hessian_diagonal = (int32_t)std::strtol(v, &end, 10);
-        else if (a == "--parent_selection") {
-            const std::string s = v;
-            if (s != "best" && s != "random") return fail(TOMO_EINVAL, "--parent_selection must be best or random");
-            p->parent_best = s == "best";
-            continue;
-        } else continue;
-        if (!end || *end != '\0') return fail(TOMO_EINVAL, "bad value for " + a + ": " + v);
-    }
-    return TOMO_OK;
+    return tomo::guarded([&]() -> int {
+        if (!p || argc < 0 || (argc > 0 && !argv)) return fail(TOMO_EINVAL, "tomo_search_parse_args: NULL argument");
+        for (int i = 0; i + 1 < argc; ++i) {
+            const std::string a = argv[i] ? argv[i] : "";
+            const char* v = argv[i + 1];
+            if (!v) continue;
+            char* end = nullptr;
+            if (a == "--population_size") p->population_size = (int32_t)std::strtol(v, &end, 10);
+            else if (a == "--maximum_iterations") p->maximum_iterations = (int32_t)std::strtol(v, &end, 10);
+            else if (a == "--seed") p->seed = (uint64_t)std::strtoull(v, &end, 0);
+            else if (a == "--inertia") p->inertia = std::strtod(v, &end);
+            else if (a == "--local_best_weight") p->local_best_weight = std::strtod(v, &end);
+            else if (a == "--global_best_weight") p->global_best_weight = std::strtod(v, &end);
+            else if (a == "--crossover_rate") p->crossover_rate = std::strtod(v, &end);
+            else if (a == "--differential_scale") p->differential_scale = std::strtod(v, &end);
+            else if (a == "--number_pairs") p->number_pairs = (int32_t)std::strtol(v, &end, 10);
+            else if (a == "--regression_size") p->regression_size = (int32_t)std::strtol(v, &end, 10);
+            else if (a == "--line_search_size") p->line_search_size = (int32_t)std::strtol(v, &end, 10);
+            else if (a == "--line_search_min") p->line_search_min = std::strtod(v, &end);
+            else if (a == "--line_search_max") p->line_search_max = std::strtod(v, &end);
+            else if (a == "--hessian_diagonal") p->hessian_diagonal = (int32_t)std::strtol(v, &end, 10);
+            else if (a == "--parent_selection") {
+                const std::string s = v;
+                if (s != "best" && s != "random") return fail(TOMO_EINVAL, "--parent_selection must be best or random");
+                p->parent_best = s == "best";
+                continue;
+            } else continue;
+            if (!end || *end != '\0') return fail(TOMO_EINVAL, "bad value for " + a + ": " + v);
+        }
+        return TOMO_OK;
+    });
 }
 
 int tomo_search_run(const tomo_search_params* p, const double* min_bound, const double* max_bound, size_t n_param,
                     tomo_batch_fitness_fn f, void* user, tomo_generation_fn report, void* report_user,
                     double* best_params, double* best_fitness, double* history, int64_t* evaluations) {
-    if (!p || !min_bound || !max_bound || !f || !best_params || !best_fitness)
-        return fail(TOMO_EINVAL, "tomo_search_run: NULL argument");
-    if (p->type != TOMO_SEARCH_PS && p->type != TOMO_SEARCH_DE && p->type != TOMO_SEARCH_ANM)
-        return fail(TOMO_EINVAL, "unknown search type");
-    if (n_param < 1) return fail(TOMO_EINVAL, "no parameters");
-    for (size_t j = 0; j < n_param; ++j)
-        if (!std::isfinite(min_bound[j]) || !std::isfinite(max_bound[j]) || max_bound[j] < min_bound[j])
-            return fail(TOMO_EINVAL, "bounds must be finite with min <= max");
-    if (p->type != TOMO_SEARCH_ANM && p->population_size < 4)
-        return fail(TOMO_EINVAL, "population_size must be at least 4");
-    if (p->type == TOMO_SEARCH_ANM &&
-        (p->line_search_size < 2 || p->regression_size < 0 || !(p->line_search_max > p->line_search_min)))
-        return fail(TOMO_EINVAL, "line_search_size must be >= 2 and line_search_max above line_search_min");
-    if (p->maximum_iterations < 0) return fail(TOMO_EINVAL, "maximum_iterations must be >= 0");
-    if (p->type == TOMO_SEARCH_DE && (p->number_pairs < 1 || p->population_size < 2 * p->number_pairs + 2))
-        return fail(TOMO_EINVAL, "population too small for the number of difference pairs");
-    Run R{*p, min_bound, max_bound, n_param, f, user, report, report_user};
-    Rng g(p->seed);
-    const int rc = p->type == TOMO_SEARCH_PS   ? particle_swarm(R, g, best_params, best_fitness, history)
-                   : p->type == TOMO_SEARCH_DE ? differential_evolution(R, g, best_params, best_fitness, history)
-                                               : newton_method(R, g, best_params, best_fitness, history);
-    if (evaluations) *evaluations = R.evals;
-    return rc;
+    return tomo::guarded([&]() -> int {
+        if (!p || !min_bound || !max_bound || !f || !best_params || !best_fitness)
+            return fail(TOMO_EINVAL, "tomo_search_run: NULL argument");
+        if (p->type != TOMO_SEARCH_PS && p->type != TOMO_SEARCH_DE && p->type != TOMO_SEARCH_ANM)
+            return fail(TOMO_EINVAL, "unknown search type");
+        if (n_param < 1) return fail(TOMO_EINVAL, "no parameters");
+        for (size_t j = 0; j < n_param; ++j)
+            if (!std::isfinite(min_bound[j]) || !std::isfinite(max_bound[j]) || max_bound[j] < min_bound[j])
+                return fail(TOMO_EINVAL, "bounds must be finite with min <= max");
+        if (p->type != TOMO_SEARCH_ANM && p->population_size < 4)
+            return fail(TOMO_EINVAL, "population_size must be at least 4");
+        if (p->type == TOMO_SEARCH_ANM &&
+            (p->line_search_size < 2 || p->regression_size < 0 || !(p->line_search_max > p->line_search_min)))
+            return fail(TOMO_EINVAL, "line_search_size must be >= 2 and line_search_max above line_search_min");
+        if (p->maximum_iterations < 0) return fail(TOMO_EINVAL, "maximum_iterations must be >= 0");
+        if (p->type == TOMO_SEARCH_DE && (p->number_pairs < 1 || p->population_size < 2 * p->number_pairs + 2))
+            return fail(TOMO_EINVAL, "population too small for the number of difference pairs");
+        Run R{*p, min_bound, max_bound, n_param, f, user, report, report_user};
+        Rng g(p->seed);
+        const int rc = p->type == TOMO_SEARCH_PS   ? particle_swarm(R, g, best_params, best_fitness, history)
+                       : p->type == TOMO_SEARCH_DE ? differential_evolution(R, g, best_params, best_fitness, history)
+                                                   : newton_method(R, g, best_params, best_fitness, history);
+        if (evaluations) *evaluations = R.evals;
+        return rc;
+    });
 }
 
 }  // extern "C"
