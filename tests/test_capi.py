@@ -164,3 +164,58 @@ def test_dropin_target_file_rules(tomo, tmp_path):
         assert ei.value.status == -1, name
     with pytest.raises(tomo.TomoError):
         tomo._target_values(meas[:5000])
+
+
+C_PROGRAM = r"""
+#include "tomography.h"
+#include <stdio.h>
+static int bowl(void *user, const double *pop, size_t n, size_t np, double *fit) {
+    (void)user;
+    for (size_t i = 0; i < n; ++i) {
+        double s = 0;
+        for (size_t j = 0; j < np; ++j) { double d = pop[i * np + j] - 0.25; s += d * d; }
+        fit[i] = -s;
+    }
+    return TOMO_OK;
+}
+int main(void) {
+    tomo_spec s;
+    if (tomo_spec_breast(&s, 1) != TOMO_OK) return 1;
+    tomo_search_params p;
+    const char *argv[] = {"--population_size", "20", "--maximum_iterations", "60", "--seed", "3"};
+    if (tomo_search_defaults(&p, TOMO_SEARCH_DE) || tomo_search_parse_args(&p, 6, argv)) return 2;
+    double lo[4] = {-1, -1, -1, -1}, hi[4] = {1, 1, 1, 1}, best[4], fit;
+    int64_t evals = 0;
+    int rc = tomo_search_run(&p, lo, hi, 4, bowl, NULL, NULL, NULL, best, &fit, NULL, &evals);
+    printf("%d %d %lld %.17g\n", tomo_num_params(&s), rc, (long long)evals, fit);
+    return rc;
+}
+"""
+
+
+def test_c_header_is_c99_and_links(tomo, tmp_path):
+    """include/tomography.h is a C header (strict C99, no warnings), and a C
+    caller links the library and runs a search through it with a C callback;
+    the tao-style C++ caller of the drop-in (a double (*)(const
+    std::vector<double>&) bound to FDTD_GPU) compiles and links."""
+    import shutil
+    import subprocess
+
+    cc, cxx = shutil.which("gcc") or shutil.which("cc"), shutil.which("g++") or shutil.which("c++")
+    if cc is None or cxx is None:
+        pytest.skip("no C/C++ compiler")
+    lib_dir = os.path.dirname(tomo.LIB_PATH)
+    inc = os.path.join(REPO, "include")
+    link = ["-L", lib_dir, "-ltomography_gb300", "-Wl,-rpath," + lib_dir]
+    src = tmp_path / "caller.c"
+    src.write_text(C_PROGRAM)
+    exe = tmp_path / "caller"
+    subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic", "-I", inc, str(src), "-o", str(exe)]
+                   + link, check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+    assert out[:3] == ["64", "0", str(20 * 61)] and float(out[3]) > -1e-6
+    cpp = tmp_path / "dropin.cpp"
+    cpp.write_text('#include "tomography_fdtd.hpp"\n#include <vector>\n'
+                   'int main() { double (*f)(const std::vector<double>&) = FDTD_GPU; return f == nullptr; }\n')
+    subprocess.run([cxx, "-std=c++17", "-Wall", "-Werror", "-I", inc, str(cpp), "-o", str(tmp_path / "dropin")]
+                   + link, check=True)
