@@ -402,13 +402,16 @@ int oracle_solve_many(const oracle_problem *probs, int n, int nthreads) {
 
 /* ------------------------------------------------------------- far field */
 void oracle_far_field(int nx, int ny, int d, double dx, int nfreq, const double *freqs, const double *acc,
-                      int nangle, int norm, double tau, double *D, double *P) {
-    /* N2FPostProcess, FDTD_GPU.cu:553-634; calc_incident_power FDTD_common.cxx:48-51 */
-    const double c0 = 1.0 / sqrt(MU0_D * EPS0_D), eta0 = sqrt(MU0_D / EPS0_D);
+                      int nangle, int norm, double tau, double nbg, double *D, double *P) {
+    /* N2FPostProcess, FDTD_GPU.cu:553-634; calc_incident_power FDTD_common.cxx:48-51.
+       The reference transforms in vacuum (nbg = 1); the breast mode's contour
+       lies in its lossless background, whose wavenumber and impedance are
+       nbg k0 and eta0 / nbg. */
+    const double c0 = 1.0 / sqrt(MU0_D * EPS0_D), eta0 = sqrt(MU0_D / EPS0_D), eta = eta0 / nbg;
     const int C = oracle_contour_size(nx, ny, d);
     const double cxo = nx / 2.0 - 1, cyo = ny / 2.0 - 1;
     for (int f = 0; f < nfreq; ++f) {
-        const double fr = freqs[f], k = 2 * PI_D * fr / c0;
+        const double fr = freqs[f], k = 2 * PI_D * fr * nbg / c0;
         const double *a = acc + (size_t)f * C * 4;
         double prad = 1.0;
         if (norm == 1) {
@@ -435,8 +438,8 @@ void oracle_far_field(int nx, int ny, int d, double dx, int nfreq, const double 
                 Lr += wt * (mr * er - mi * ei) * dx;
                 Li += wt * (mr * ei + mi * er) * dx;
             }
-            double Er = Lr + eta0 * Nr, Ei = Li + eta0 * Ni;
-            D[(size_t)f * nangle + ai] = k * k * (Er * Er + Ei * Ei) / (8 * PI_D * eta0 * prad);
+            double Er = Lr + eta * Nr, Ei = Li + eta * Ni;
+            D[(size_t)f * nangle + ai] = k * k * (Er * Er + Ei * Ei) / (8 * PI_D * eta * prad);
             P[(size_t)f * nangle + ai] = atan2(Ei, Er);
         }
     }

@@ -99,11 +99,13 @@ int oracle_solve_many(const oracle_problem *probs, int n, int nthreads);
 int oracle_contour_size(int nx, int ny, int d);
 void oracle_contour_point(int nx, int ny, int d, int index, int *x, int *y, int *face);
 
-/* Far field from the DFT accumulators, D/P laid out [nfreq][nangle].
-   norm = 0: D = k^2 |L + eta0 N|^2 / (8 pi eta0)
+/* Far field from the DFT accumulators, D/P laid out [nfreq][nangle], in a
+   background of refractive index nbg (k = nbg k0, eta = eta0 / nbg; 1 for the
+   reference's vacuum):
+   norm = 0: D = k^2 |L + eta N|^2 / (8 pi eta)
    norm = 1: reference normalisation, additionally / (Prad(f) * 33.329)   */
 void oracle_far_field(int nx, int ny, int d, double dx, int nfreq, const double *freqs, const double *acc,
-                      int nangle, int norm, double tau, double *D, double *P);
+                      int nangle, int norm, double tau, double nbg, double *D, double *P);
 
 /* CPML profile (FDTD_GPU.cu:748-806), out = [6][ncpml] as in oracle_problem */
 void oracle_cpml_profile(int ncpml, double grading, double sigma_max, double kappa_max, double alpha_max,

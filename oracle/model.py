@@ -64,7 +64,7 @@ def lib(bits: int = 64) -> C.CDLL:
         L.oracle_contour_size.argtypes = [C.c_int, C.c_int, C.c_int]
         L.oracle_contour_point.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _ip, _ip, _ip]
         L.oracle_far_field.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, _dp, _dp, C.c_int, C.c_int,
-                                       C.c_double, _dp, _dp]
+                                       C.c_double, C.c_double, _dp, _dp]
         L.oracle_cpml_profile.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                           C.c_double, C.c_double, _dp]
         L.oracle_material_coefs.argtypes = [C.c_double] * 6 + [_dp, _dp]
@@ -283,8 +283,11 @@ def far_field(pr: Problem, norm: int, tau: float, nangle: int, bits: int = 64) -
     D = np.zeros((F, nangle))
     P = np.zeros((F, nangle))
     freqs = np.array(s["freqs"][:F], dtype=np.float64)
+    # the breast mode's contour lies in its lossless background (refractive
+    # index sqrt(bg_eps_inf)); the reference modes transform in vacuum
+    nbg = math.sqrt(s["bg_eps_inf"]) if s.get("mode") == 2 else 1.0
     lib(bits).oracle_far_field(pr.p.nx, pr.p.ny, pr.p.nf_d, pr.p.dx, F, _d(freqs), _d(pr.acc), nangle, norm, tau,
-                               _d(D), _d(P))
+                               nbg, _d(D), _d(P))
     return D, P
 
 

@@ -36,7 +36,7 @@ def _rank_main(rank: int, world: int, port: int, out: dict):
 
 def test_two_gloo_ranks_take_disjoint_candidates_and_max_time():
     port = _free_port()
-    with mp.Manager() as mgr:
+    with mp.get_context("spawn").Manager() as mgr:   # no fork of this (threaded) process
         out = mgr.dict()
         mp.spawn(_rank_main, args=(2, port, out), nprocs=2, join=True)
         res = dict(out)

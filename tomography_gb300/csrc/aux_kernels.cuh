@@ -103,15 +103,17 @@ __global__ void farfield_kernel(const Real* __restrict__ acc, size_t acc_stride,
                                 int nfreq,
                                 const double* __restrict__ freqs, const double* __restrict__ geom,
                                 const double* __restrict__ ang, int nang, double dl, int norm, double tau,
-                                float* __restrict__ D, float* __restrict__ P) {
+                                double nbg, float* __restrict__ D, float* __restrict__ P) {
     // geom[c] = (X, Y, face) [m]; ang[a] = (cos phi, sin phi); sums in Real.
+    // nbg: refractive index of the lossless background the contour lies in
+    // (k = nbg k0, eta = eta0 / nbg); 1 for the reference's vacuum transform.
     // inc (total field, may be null): the incident grid's accumulators, added to
     // every solve's own (the legacy's single sum of both, by linearity).
     const int s = blockIdx.y, f = blockIdx.x;
     const Real* a = acc + (size_t)s * acc_stride + (size_t)f * C * 8;
     const Real* ia = inc ? inc + (size_t)f * C * 8 : nullptr;
-    const double c0 = 1.0 / sqrt(kMu0D * kEps0D), eta0 = sqrt(kMu0D / kEps0D);
-    const double fr = freqs[f], k = 2 * kPiD * fr / c0;
+    const double c0 = 1.0 / sqrt(kMu0D * kEps0D), eta0 = sqrt(kMu0D / kEps0D), eta = eta0 / nbg;
+    const double fr = freqs[f], k = 2 * kPiD * fr * nbg / c0;
     double prad = 1.0;
     if (norm == 1) {
         double g = tau * sqrt(kPiD) * exp(-tau * tau * 2 * kPiD * fr * 2 * kPiD * fr / 4);
@@ -148,9 +150,9 @@ __global__ void farfield_kernel(const Real* __restrict__ acc, size_t acc_stride,
             Li += __shfl_xor_sync(0xffffffffu, Li, o);
         }
         if (lane == 0) {
-            const double Er = ((double)Lr + eta0 * (double)Nr) * dl, Ei = ((double)Li + eta0 * (double)Ni) * dl;
+            const double Er = ((double)Lr + eta * (double)Nr) * dl, Ei = ((double)Li + eta * (double)Ni) * dl;
             const size_t o = ((size_t)s * nfreq + f) * nang + ai;
-            D[o] = (float)(k * k * (Er * Er + Ei * Ei) / (8 * kPiD * eta0 * prad));
+            D[o] = (float)(k * k * (Er * Er + Ei * Ei) / (8 * kPiD * eta * prad));
             P[o] = (float)atan2(Ei, Er);
         }
     }

@@ -339,7 +339,8 @@ int post_range(const ClassData<Real>& cd, size_t ncand, const SolveDesc<Real>& f
         dim3 grd(pc.nfreq, nsolves);
         farfield_kernel<Real><<<grd, 256, 0, st>>>(first.acc, stride, inc_acc, pc.C, pc.nfreq, cd.freqs.template as<double>(),
                                                    cd.ffgeom.template as<double>(), cd.ffang.template as<double>(),
-                                                   pc.nang, s.dx, s.ff_norm, s.pw_tau, d_D, d_P);
+                                                   pc.nang, s.dx, s.ff_norm, s.pw_tau,
+                                                   s.mode == TOMO_MODE_BREAST ? std::sqrt(s.bg_eps_inf) : 1.0, d_D, d_P);
         ++*kernels;
     }
     if (want_fit) {
