@@ -76,7 +76,9 @@ typedef struct tomo_spec {
     int32_t n_tx;              /* transmitters fired per candidate (<= n_antennas)   */
     double antenna_radius;     /* [m]                                                */
     double src_f0, src_tau, src_t0, src_amp;  /* modulated Gaussian current source; amp 0 = auto */
-    /* near-to-far-field transform */
+    /* near-to-far-field transform: in vacuum for the reference modes, in the
+       background medium (k = sqrt(bg_eps_inf) k0, eta = eta0 / sqrt(bg_eps_inf))
+       for the breast mode, whose contour lies in that lossless background */
     int32_t nf2ff_d;           /* contour distance from the grid edge [cells]        */
     int32_t nfreq;
     double freqs[TOMO_MAX_FREQS];
