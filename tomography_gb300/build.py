@@ -39,8 +39,6 @@ SOURCES = [
     "noalloc.cu",
     "plain.cu",
 ]
-HEADERS = ["solve_desc.h", "fdtd_advance.cuh", "aux_kernels.cuh", "engine.h", "engine_impl.cuh", "plain_kernels.cuh",
-           "advance_inst.cuh"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
@@ -55,8 +53,12 @@ def nvcc() -> str:
 
 
 def _deps() -> list[str]:
-    out = [os.path.join(CSRC, h) for h in HEADERS if os.path.exists(os.path.join(CSRC, h))]
-    out.append(os.path.join(REPO, "include", "tomography.h"))
+    """Every header a translation unit may include (csrc/*.h, *.cuh and the
+    public include/ headers) and this script: a change to any of them
+    rebuilds every object."""
+    out = []
+    for d, exts in ((CSRC, (".h", ".cuh", ".hpp")), (os.path.join(REPO, "include"), (".h", ".hpp"))):
+        out += sorted(os.path.join(d, f) for f in os.listdir(d) if f.endswith(exts))
     out.append(__file__)
     return out
 
