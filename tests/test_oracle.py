@@ -549,3 +549,21 @@ def test_oracle_far_field_of_a_line_source_is_isotropic(tomo, oracle):
         D = oracle.breast_forward(spec, np.zeros(0), bits=64)["D"][0]
         assert D.shape == (3, 72) and np.all(D > 0)
         assert np.all(D.max(axis=1) / D.min(axis=1) - 1 < 0.2), (radius, D.max(axis=1) / D.min(axis=1))
+
+
+def test_source_spectrum(oracle):
+    """The breast mode's transmitter waveform (a Gaussian-modulated 6 GHz sine,
+    sampled at (n + 1/2) dt) at dx = 0.5 mm, workloads 0 and 1: zero mean,
+    spectrum peak at 6 GHz, and the -20 dB band ending at fmax =
+    c0 / (20 dx sqrt(eps_r)), the 20-cells-per-wavelength limit of the
+    background."""
+    for cfg in (0, 1):
+        s = oracle.breast_spec(cfg)
+        w = oracle.source_wave(s)
+        spec = np.abs(np.fft.rfft(w, 1 << 18))
+        f = np.fft.rfftfreq(1 << 18, s["dt"])
+        band = f[spec >= 0.1 * spec.max()]
+        fmax = 299792458.0 / (20 * s["dx"] * np.sqrt(s["bg_eps_inf"]))
+        assert abs(w.sum()) < 1e-6 * np.abs(w).max()
+        assert abs(f[np.argmax(spec)] / 6e9 - 1) < 0.01
+        assert abs(band.max() / fmax - 1) < 0.01 and band.min() > 1.5e9
