@@ -66,3 +66,41 @@ def test_row_segments_cover_every_cell_once(tomo, nseg):
                 for y in range(y0, y1):
                     cover[x][y] += 1
         assert all(v == 1 for col in cover for v in col), (nx, ny, nseg)
+
+
+def _blockings(lib, precision, mode):
+    f = lib.tomo_internal_blockings
+    f.restype, f.argtypes = C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int), C.c_int]
+    buf = (C.c_int * 512)()
+    n = f(precision, mode, buf, 512)
+    assert n > 0, lib.tomo_last_error()
+    return [tuple(buf[4 * i + j] for j in range(4)) for i in range(n)]
+
+
+SMEM_PER_SM = 228 * 1024          # sm_100 family: 228 KB per SM, 1 KB of it reserved per resident block
+SMEM_PER_BLOCK = 227 * 1024
+
+
+def test_offered_blockings_are_launchable(tomo):
+    """Every blocking the autotuner offers has a compiled kernel and a block
+    small enough to launch; the FP32 variants' requested blocks per SM (the
+    MINB their registers were capped for) also fit the SM's shared memory,
+    so the cap buys the occupancy it was made for.  The bench's blockings
+    (T 4 COLS 2 MINB 2, T 2 COLS 2 MINB 3) are offered in the breast mode, and
+    the autotuner's first choice there is T 2 COLS 2 MINB 3."""
+    lib = tomo.library()
+    for prec in (tomo.FP32, tomo.FP64):
+        for mode in (0, 1, 2):
+            bs = _blockings(lib, prec, mode)
+            for T, cols, minb, smem in bs:
+                assert 0 < smem <= SMEM_PER_BLOCK, (prec, mode, T, cols, smem)
+                if prec == tomo.FP32:
+                    assert minb * (smem + 1024) <= SMEM_PER_SM, (mode, T, cols, minb, smem)
+                else:
+                    assert cols == 1
+    breast = [b[:3] for b in _blockings(lib, tomo.FP32, 2)]
+    assert breast[0] == (2, 2, 3) and (4, 2, 2) in breast and len(breast) == len(set(breast))
+    # FP64, T 2, MINB 3: three blocks need 3 x 81.8 KB > 228 KB, so shared memory
+    # holds it to two; the autotuner times it beside MINB 2 and keeps the faster
+    f64 = {b[:3]: b[3] for b in _blockings(lib, tomo.FP64, 2)}
+    assert 3 * (f64[(2, 1, 3)] + 1024) > SMEM_PER_SM

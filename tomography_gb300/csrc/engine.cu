@@ -870,6 +870,31 @@ int create_engine(const tomo_spec* spec, EngineBase** out) {
 
 }  // namespace tomo
 
+// Internal test hook (not part of the public ABI): the blockings the
+// autotuner offers for a precision and mode, in preference order, as
+// (T, cols, minb, dynamic shared memory per block in bytes) records.  Returns
+// the count, or a negative status.
+extern "C" int tomo_internal_blockings(int precision, int mode, int* out, int cap) {
+    return tomo::guarded([&]() -> int {
+        tomo_spec s{};
+        s.mode = mode;
+        const int am = tomo::advance_mode(s);
+        std::vector<int> rec;
+        auto put = [&](const std::vector<tomo::Blocking>& bs, bool f64) {
+            for (const tomo::Blocking& b : bs) {
+                const size_t smem = f64 ? tomo::advance_smem_bytes<double>(b.T, b.cols)
+                                        : tomo::advance_smem_bytes<float>(b.T, b.cols);
+                rec.insert(rec.end(), {b.T, b.cols, b.minb, (int)smem});
+            }
+        };
+        if (precision == TOMO_FP64) put(tomo::tune_candidates<double>(am, 0, 0, 0), true);
+        else put(tomo::tune_candidates<float>(am, 0, 0, 0), false);
+        if (!out || (int)rec.size() > cap) return tomo::fail(TOMO_EINVAL, "blocking buffer too small");
+        std::copy(rec.begin(), rec.end(), out);
+        return (int)(rec.size() / 4);
+    });
+}
+
 // Internal test hook (not part of the public ABI): the work items the engine
 // launches for one solve of an nx x ny grid cut into nseg row segments, as
 // (x0, x1, narrow, y0, y1) records, after the same host validation.  Returns
