@@ -567,3 +567,41 @@ def test_source_spectrum(oracle):
         assert abs(w.sum()) < 1e-6 * np.abs(w).max()
         assert abs(f[np.argmax(spec)] / 6e9 - 1) < 0.01
         assert abs(band.max() / fmax - 1) < 0.01 and band.min() > 1.5e9
+
+
+def test_oracle_discrete_energy(tomo, oracle):
+    """Known answer: the Yee scheme in a closed PEC cavity (no CPML) filled
+    with a lossless medium conserves W(n) = eps |Ez(n)|^2 + mu0 <H(n-1/2),
+    H(n+1/2)> exactly once the source has died out: W(n+1) - W(n) =
+    (eps Cb - mu0 chez) (...) = 0.  Here W stays constant to 1e-12 from step
+    1000 to 2500, while the naive eps |E|^2 + mu0 |H|^2 of one time level
+    swings by 0.4 %.  eps is 9 x the reference's eps0 = 8.85418e-12
+    (FDTD_common.hxx:6), the value the coefficients are built from; with the
+    CODATA eps0 W would drift at 1e-7.  A conductive filling (sigma 0.05 S/m)
+    gives W(n+1) - W(n) = -sigma dt |(E(n+1) + E(n))/2|^2 < 0: W falls at every
+    step."""
+    mu0, eps0_ref = 4e-7 * np.pi, 8.85418e-12
+    spec = tomo.breast_spec(0).copy(nx=100, ny=100, steps=3000, ncpml=0, nf2ff_d=5, disc_radius=0.0,
+                                    n_ellipses=0, n_antennas=8, n_tx=1, antenna_radius=15e-3, nfreq=0).as_dict()
+    eps = spec["bg_eps_inf"] * eps0_ref
+
+    def fields(params, n):
+        pr = oracle.breast_problem(spec, params, 0, n)
+        pr.want_fields()
+        oracle.run([pr])
+        return pr.ez.copy(), pr.hx.copy(), pr.hy.copy()
+
+    def energy(params, n):
+        ez, hx, hy = fields(params, n)
+        _, hx1, hy1 = fields(params, n + 1)
+        return eps * np.sum(ez ** 2) + mu0 * np.sum(hx * hx1 + hy * hy1), \
+            eps * np.sum(ez ** 2) + mu0 * np.sum(hx ** 2 + hy ** 2)
+
+    none = np.zeros(0)
+    W = [energy(none, n) for n in (1000, 1001, 1700, 2500)]
+    exact, naive = np.array([w[0] for w in W]), np.array([w[1] for w in W])
+    assert np.ptp(exact) <= 1e-12 * exact[0]
+    assert np.ptp(naive) > 1e-3 * naive[0]
+    lossy = np.array([0.0, 0.0, 1.0, 1.0, 0.0, spec["bg_eps_inf"], 0.0, 0.05])   # a 1 m circle: the whole cavity
+    Wl = [energy(lossy, n)[0] for n in (1000, 1001, 1002, 1500)]
+    assert all(b < a for a, b in zip(Wl, Wl[1:])) and Wl[-1] < 0.9 * Wl[0]
