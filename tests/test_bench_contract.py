@@ -11,6 +11,8 @@ import os
 import subprocess
 import sys
 
+import pytest
+
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
@@ -20,10 +22,25 @@ def _run(env_extra):
                            "--warmup", "0"], capture_output=True, text=True, env=env, timeout=600, cwd=REPO)
 
 
-def test_reference_arm_json_line():
-    out = _run({})
+@pytest.fixture(scope="module")
+def reference_run():
+    """One run of the reference arm (rank 0, one step) in a fresh interpreter,
+    shared by the tests below: its printed lines, and whether the product
+    package was imported or its native library mapped into the process."""
+    code = ("import sys; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '0'];"
+            "sys.path.insert(0, %r); import bench; bench.main();"
+            "maps = open('/proc/self/maps').read();"
+            "print('PRODUCT', any(m.startswith('tomography_gb300') for m in sys.modules),"
+            " 'libtomography_gb300' in maps)") % REPO
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=REPO, env=env)
     assert out.returncode == 0, out.stderr
     lines = [l for l in out.stdout.splitlines() if l.strip()]
+    return [l for l in lines if not l.startswith("PRODUCT")], [l for l in lines if l.startswith("PRODUCT")]
+
+
+def test_reference_arm_json_line(reference_run):
+    lines, _ = reference_run
     assert len(lines) == 1
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["metric"] == "PSO fitness evals/s" and d["unit"] == "evals/s"
@@ -39,26 +56,18 @@ def test_reference_arm_other_ranks_are_silent():
     assert out.returncode == 0 and out.stdout.strip() == ""
 
 
-def test_reference_arm_does_not_load_the_product():
+def test_reference_arm_does_not_load_the_product(reference_run):
     """The reference arm runs the checker only: the product package is never
     imported and its native library never mapped into the process."""
-    code = ("import sys; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '0'];"
-            "sys.path.insert(0, %r); import bench; bench.main();"
-            "maps = open('/proc/self/maps').read();"
-            "print('PRODUCT', any(m.startswith('tomography_gb300') for m in sys.modules),"
-            " 'libtomography_gb300' in maps)") % REPO
-    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=REPO)
-    assert out.returncode == 0, out.stderr
-    tail = [l for l in out.stdout.splitlines() if l.startswith("PRODUCT")]
-    assert tail == ["PRODUCT False False"], out.stdout[-500:]
+    _, tail = reference_run
+    assert tail == ["PRODUCT False False"], tail
 
 
-def test_both_arms_report_the_same_config():
+def test_both_arms_report_the_same_config(reference_run):
     sys.path.insert(0, REPO)
     import bench
 
-    out = _run({})
-    d = json.loads([l for l in out.stdout.splitlines() if l.strip()][0])
+    d = json.loads(reference_run[0][0])
     assert d["config"] == bench.workload_config(1, bench.N_CAND)
 
 
