@@ -219,3 +219,30 @@ def test_c_header_is_c99_and_links(tomo, tmp_path):
                    'int main() { double (*f)(const std::vector<double>&) = FDTD_GPU; return f == nullptr; }\n')
     subprocess.run([cxx, "-std=c++17", "-Wall", "-Werror", "-I", inc, str(cpp), "-o", str(tmp_path / "dropin")]
                    + link, check=True)
+
+
+def test_python_signatures_match_the_c_header(tomo):
+    """The ctypes binding declares each C function with as many arguments as
+    include/tomography.h and the drop-in header give it, and a void return
+    exactly where the header has one."""
+    text = ""
+    for fn in ("tomography.h", "tomography_fdtd.hpp"):
+        text += open(os.path.join(REPO, "include", fn)).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = re.sub(r"//[^\n]*", "", text)
+    text = re.sub(r"typedef\s+[^;{}]*\(\s*\*[^;{}]*;", "", text)
+    protos = {}
+    for m in re.finditer(r"\b(int|void|const char\s*\*)\s*(tomo_\w+)\s*\(([^;{}]*)\)\s*;", text):
+        params = m.group(3).strip()
+        n = 0 if params in ("", "void") else params.count(",") + 1
+        protos[m.group(2)] = (m.group(1).strip(), n)
+    lib = tomo.library()
+    checked = 0
+    for name, (ret, n) in protos.items():
+        fn = getattr(lib, name)
+        if fn.argtypes is None:
+            continue                                  # not bound in Python
+        assert len(fn.argtypes) == n, (name, len(fn.argtypes), n)
+        assert (fn.restype is None) == (ret == "void"), name
+        checked += 1
+    assert checked >= 30 and "tomo_search_run" in protos and "tomo_wait" in protos
