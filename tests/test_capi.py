@@ -246,3 +246,38 @@ def test_python_signatures_match_the_c_header(tomo):
         assert (fn.restype is None) == (ret == "void"), name
         checked += 1
     assert checked >= 30 and "tomo_search_run" in protos and "tomo_wait" in protos
+
+
+def test_ctypes_structs_match_the_c_layout(tomo, tmp_path):
+    """Every ctypes mirror of a C struct (tomo_spec, tomo_outputs, tomo_stats,
+    tomo_search_params) has the C struct's size and each field at the C
+    offset: a C program compiled against include/tomography.h prints
+    sizeof/offsetof for the fields the mirrors name."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    from tomography_gb300.spec import Spec
+
+    mirrors = {"tomo_spec": Spec, "tomo_outputs": tomo.Outputs, "tomo_stats": tomo.Stats,
+               "tomo_search_params": tomo.SearchParams}
+    lines = ['#include "tomography.h"', "#include <stddef.h>", "#include <stdio.h>", "int main(void) {"]
+    for cname, py in mirrors.items():
+        lines.append(f'    printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f in py._fields_:
+            lines.append(f'    printf("{cname} {f[0]} %zu\\n", offsetof({cname}, {f[0]}));')
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c99", "-I", os.path.join(REPO, "include"), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines():
+        cname, field, value = line.split()
+        got[(cname, field)] = int(value)
+    for cname, py in mirrors.items():
+        assert C.sizeof(py) == got[(cname, "size")], cname
+        for f in py._fields_:
+            assert getattr(py, f[0]).offset == got[(cname, f[0])], (cname, f[0])
