@@ -1,10 +1,18 @@
-"""CPU: the oracle (C restatement) pinned against the reference's own CPU code.
+"""CPU: the oracle (C restatement) pinned against the reference's own code,
+and against known answers of the physics.
 
 The golden fixtures were produced by the reference's FDTD_CPU.cxx functions
-(tests/golden/make_golden.py).  The oracle in FP64 must reproduce them to
+(tests/golden/make_golden.py) and by its FDTD_GPU.cu run unchanged on a GB300
+(tests/golden/make_golden_gpu.py).  The oracle in FP64 must reproduce them to
 FP32 accuracy: the reference computes in float, so fields / probe traces agree
 to rel-L2 <= 1e-5 and far-field D to max error <= 1e-5 of max |D| after 1000
 steps (measured: ~3e-6 and ~2e-6).
+
+Known answers that need no reference run: mirror symmetry, source linearity
+and reciprocity of the traces; free-space delay and 1/sqrt(r) spreading;
+CPML reflection; the analytic Debye medium (second-order convergence); an
+isotropic far field; exact discrete energy conservation in a PEC cavity;
+the transmitter spectrum.
 """
 from __future__ import annotations
 
