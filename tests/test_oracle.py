@@ -446,6 +446,29 @@ def _homogeneous_spec(tomo, n, ncpml, steps, radius):
                                     n_antennas=16, n_tx=1, antenna_radius=radius, nfreq=0).as_dict()
 
 
+def free_space_fit(traces, spec, oracle):
+    """(slope x v, intercept - t0 in steps, relative spread of amplitude x
+    sqrt(r)) of the envelope peaks of one transmitter's receivers: the
+    Hilbert envelope's maximum, refined by a parabola, fitted as t = t0 + r/v
+    over the receivers more than 20 mm away (kr > 7)."""
+    from scipy import signal
+
+    ant = oracle.antenna_cells(spec)
+    r = np.hypot(*(ant - ant[0]).T) * spec["dx"]
+    env = np.abs(signal.hilbert(np.asarray(traces, dtype=np.float64), axis=1))
+    peak = []
+    for e in env:
+        i = int(np.argmax(e))
+        y0, y1, y2 = e[i - 1:i + 2]
+        peak.append((i + 0.5 * (y0 - y2) / (y0 - 2 * y1 + y2)) * spec["dt"])
+    peak = np.array(peak)
+    far = r > 20e-3
+    slope, t0 = np.polyfit(r[far], peak[far], 1)
+    v = 299792458.0 / np.sqrt(spec["bg_eps_inf"])
+    a = env.max(axis=1)[far] * np.sqrt(r[far])
+    return slope * v, (t0 - spec["src_t0"]) / spec["dt"], np.std(a) / np.mean(a)
+
+
 def test_oracle_free_space_propagation(tomo, oracle):
     """Known answer: in a homogeneous lossless medium the pulse of a line
     source arrives at distance r after r / v, v = c0 / sqrt(eps_r), and its
@@ -455,25 +478,13 @@ def test_oracle_free_space_propagation(tomo, oracle):
     2 % of 1/v (measured 0.7 % slower: grid dispersion at 33 cells per
     wavelength), the intercept within 5 dt of t0 (measured 2.2 dt), and
     amplitude x sqrt(r) is constant to 1 % (measured 0.14 %)."""
-    signal = pytest.importorskip("scipy.signal")
+    pytest.importorskip("scipy.signal")
     spec = _homogeneous_spec(tomo, 200, 10, 1400, 30e-3)
     tr = oracle.breast_forward(spec, np.zeros(0), bits=64)["traces"][0]
-    ant = oracle.antenna_cells(spec)
-    r = np.hypot(*(ant - ant[0]).T) * spec["dx"]
-    env = np.abs(signal.hilbert(tr, axis=1))
-    peak = []
-    for e in env:
-        i = int(np.argmax(e))
-        y0, y1, y2 = e[i - 1:i + 2]
-        peak.append((i + 0.5 * (y0 - y2) / (y0 - 2 * y1 + y2)) * spec["dt"])
-    peak = np.array(peak)
-    far = r > 20e-3                                     # kr > 7: out of the near field
-    slope, t0 = np.polyfit(r[far], peak[far], 1)
-    v = 299792458.0 / np.sqrt(spec["bg_eps_inf"])
-    assert abs(slope * v - 1.0) < 0.02
-    assert abs(t0 - spec["src_t0"]) < 5 * spec["dt"]
-    a = env.max(axis=1)[far] * np.sqrt(r[far])
-    assert np.std(a) / np.mean(a) < 0.01
+    slope_v, t0_steps, spread = free_space_fit(tr, spec, oracle)
+    assert abs(slope_v - 1.0) < 0.02
+    assert abs(t0_steps) < 5
+    assert spread < 0.01
 
 
 def test_oracle_cpml_reflection(tomo, oracle):
