@@ -268,11 +268,15 @@ int newton_method(Run& R, Rng& g, double* best_params, double* best_fitness, dou
                 else
                     for (size_t b = a; b < k; ++b) phi[q++] = (a == b ? 0.5 : 1.0) * z[a] * z[b];
             }
-            for (size_t u = 0; u < nu; ++u) {
+            for (size_t u = 0; u < nu; ++u) {   // the upper triangle; mirrored below
                 rhs[u] += phi[u] * fx[i];
-                for (size_t v = 0; v < nu; ++v) A[u * nu + v] += phi[u] * phi[v];
+                const double pu = phi[u];
+                double* row = &A[u * nu];
+                for (size_t v = u; v < nu; ++v) row[v] += pu * phi[v];
             }
         }
+        for (size_t u = 0; u < nu; ++u)
+            for (size_t v = 0; v < u; ++v) A[u * nu + v] = A[v * nu + u];
         double tr = 0;
         for (size_t u = 0; u < nu; ++u) tr += A[u * nu + u];
         for (size_t u = 0; u < nu; ++u) A[u * nu + u] += 1e-12 * tr / (double)nu;
