@@ -281,3 +281,39 @@ def test_ctypes_structs_match_the_c_layout(tomo, tmp_path):
         assert C.sizeof(py) == got[(cname, "size")], cname
         for f in py._fields_:
             assert getattr(py, f[0]).offset == got[(cname, f[0])], (cname, f[0])
+
+
+def test_target_files(tomo, tmp_path):
+    """Targets round-trip through every save_target format (.npy, text, raw
+    float32) in the shape set_target takes; a file of the wrong length, with
+    non-numeric text, of a partial float32 or with non-finite values is
+    refused; a reference-mode file may hold the reference's whole array
+    (magnitudes then phases), of which the first half is the target."""
+    rng = np.random.default_rng(3)
+    spec = tomo.breast_spec(0).copy(n_tx=2, n_antennas=4, steps=50)
+    t = rng.standard_normal(tomo.target_shape(spec)).astype(np.float32)
+    for name in ("t.npy", "t.txt", "t.csv", "t.f32"):
+        path = str(tmp_path / name)
+        tomo.save_target(path, t)
+        got = tomo.load_target(path, spec)
+        assert got.shape == (2, 4, 50) and got.dtype == np.float32
+        np.testing.assert_array_equal(got, t)
+    bad = tmp_path / "short.f32"
+    t.ravel()[:-1].tofile(bad)
+    with pytest.raises(ValueError, match="values"):
+        tomo.load_target(str(bad), spec)
+    (tmp_path / "junk.txt").write_text("1.0, 2.0\n# comment\n")
+    with pytest.raises(ValueError):
+        tomo.load_target(str(tmp_path / "junk.txt"), spec)
+    (tmp_path / "odd.bin").write_bytes(b"\x00" * 10)
+    with pytest.raises(ValueError, match="float32"):
+        tomo.load_target(str(tmp_path / "odd.bin"), spec)
+    nan = t.copy()
+    nan[0, 0, 0] = np.nan
+    tomo.save_target(str(tmp_path / "nan.npy"), nan)
+    with pytest.raises(ValueError, match="non-finite"):
+        tomo.load_target(str(tmp_path / "nan.npy"), spec)
+    ref = tomo.reference_spec(False)
+    whole = rng.random(8000).astype(np.float32)
+    whole.tofile(tmp_path / "meas.f32")
+    np.testing.assert_array_equal(tomo.load_target(str(tmp_path / "meas.f32"), ref).ravel(), whole[:4000])

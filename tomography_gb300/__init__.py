@@ -380,6 +380,66 @@ _dropin: Optional[Solver] = None
 REFERENCE_TARGET_SIZE = 4000   # E * F * A of the reference preset (4 x 10 x 100)
 
 
+def target_shape(spec: Spec) -> tuple:
+    """Shape of the target Solver.set_target takes for spec: the receiver
+    traces [n_tx][n_antennas][steps] in the breast mode, the far-field
+    magnitudes [n_excitations][nfreq][n_angles] in the reference modes."""
+    if spec.mode == MODE_BREAST:
+        return (spec.n_tx, spec.n_antennas, spec.steps)
+    return (library().tomo_num_excitations(C.byref(spec)), spec.nfreq, spec.n_angles)
+
+
+def save_target(path: str, target: np.ndarray) -> None:
+    """Write a target: NumPy .npy when path ends in .npy, text (one value per
+    line) for .txt and .csv, else raw little-endian float32."""
+    t = np.ascontiguousarray(target, dtype=np.float32)
+    low = path.lower()
+    if low.endswith(".npy"):
+        np.save(path, t)
+    elif low.endswith((".txt", ".csv")):
+        np.savetxt(path, t.ravel(), fmt="%.9g")
+    else:
+        t.ravel().astype("<f4").tofile(path)
+
+
+def load_target(path: str, spec: Spec) -> np.ndarray:
+    """Read a target for spec from a file in one of save_target's formats:
+    .npy (any real dtype), text (.txt/.csv: numbers separated by spaces,
+    commas or newlines; anything else raises) or raw little-endian float32.
+    It must hold exactly the target's number of values, or in the reference
+    modes twice that (magnitudes then phases, the reference's whole array),
+    of which the first half is used.  Returns float32 in target_shape(spec)."""
+    import re
+
+    shape = target_shape(spec)
+    n = int(np.prod(shape))
+    low = path.lower()
+    if low.endswith(".npy"):
+        v = np.load(path, allow_pickle=False)
+        if not np.issubdtype(v.dtype, np.floating) and not np.issubdtype(v.dtype, np.integer):
+            raise ValueError(f"{path}: not a real-valued array")
+        v = v.astype(np.float64).ravel()
+    elif low.endswith((".txt", ".csv")):
+        with open(path, encoding="utf-8-sig") as fp:
+            tokens = [t for t in re.split(r"[\s,]+", fp.read().strip()) if t]
+        try:
+            v = np.array([float(t) for t in tokens])
+        except ValueError as e:
+            raise ValueError(f"{path}: {e}") from None
+    else:
+        raw = np.fromfile(path, dtype=np.uint8)
+        if raw.size % 4:
+            raise ValueError(f"{path}: {raw.size} bytes is not a whole number of float32 values")
+        v = raw.view("<f4").astype(np.float64)
+    if v.size == 2 * n and spec.mode != MODE_BREAST:
+        v = v[:n]
+    if v.size != n:
+        raise ValueError(f"{path}: {v.size} values, the target of this spec holds {n} {shape}")
+    if not np.all(np.isfinite(v)):
+        raise ValueError(f"{path}: non-finite values")
+    return v.astype(np.float32).reshape(shape)
+
+
 def read_target_file(path: str) -> np.ndarray:
     """The far-field target of the drop-in from a measurement file, with the
     native library's rules: raw float32 or text (numbers separated by spaces,

@@ -284,6 +284,10 @@ def main(argv=None) -> int:
     ap.add_argument("--workload", type=int, default=1, help="breast-imaging workload (0..4)")
     ap.add_argument("--target_seed_offset", type=int, default=1)
     ap.add_argument("--steps", type=int, default=0, help="override the time steps per solve")
+    ap.add_argument("--target", default=None,
+                    help="target traces from a file (.npy, .txt/.csv or raw float32; see load_target) instead of "
+                         "the workload's synthetic phantom")
+    ap.add_argument("--save_target", default=None, help="write the target traces used to this file")
     args, rest = ap.parse_known_args(argv)
 
     import tomography_gb300 as T
@@ -293,8 +297,13 @@ def main(argv=None) -> int:
     if args.steps:
         spec = spec.copy(steps=args.steps)
     K = spec.n_ellipses
-    with T.Solver(spec.copy(n_ellipses=3)) as ts:
-        target = ts.forward(W.target_phantom(args.workload, 3), traces=True, far_field=False)["traces"][0]
+    if args.target:
+        target = T.load_target(args.target, spec)
+    else:
+        with T.Solver(spec.copy(n_ellipses=3)) as ts:
+            target = ts.forward(W.target_phantom(args.workload, 3), traces=True, far_field=False)["traces"][0]
+    if args.save_target:
+        T.save_target(args.save_target, target)
     lo, hi = breast_bounds(K, spec.disc_radius)
     if args.search_type == "anm":
         search = NewtonMethod(lo, hi, 0.1 * (hi - lo), rest)
